@@ -1,0 +1,186 @@
+// common.cuh - shared definitions of the GB300 NNP kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace nnpgpu {
+
+// ---- limits of the GPU path (checked on the host when the potential is loaded)
+constexpr int NT_MAX = 4;                          // atom types
+constexpr int NB_MAX = NT_MAX * (NT_MAX + 1) / 2;  // angular blocks per centre type
+constexpr int NR_MAX = 32;                         // radial functions per (centre, neighbour) type
+constexpr int NA_MAX = 64;                         // angular functions per block
+constexpr int NE_MAX = 4;                          // distinct angular widths per block
+constexpr int NL = 2;                              // distinct lambda values per block
+constexpr int NZ_MAX = 6;                          // zeta = 2^m, m < NZ_MAX
+constexpr int NIN_MAX = 256;                       // network inputs
+constexpr int NLAYER_MAX = 4;                      // network layers (hidden + output)
+constexpr int HID_MAX = 256;                       // nodes per layer
+
+enum { CUT_STEP = 1, CUT_COS = 2, CUT_TANH = 3 };
+enum { ACT_LINEAR = 1, ACT_SIGMOID = 2, ACT_TANH = 3 };
+
+// Radial basis of centre type I against neighbour type J (BasisR, src/nnp/basis_radial.hpp:53-94).
+struct RadialP {
+  int n, off, cut, pad;
+  float rc, pirc, rci, norm;
+  float rs[NR_MAX], eta[NR_MAX];
+};
+
+// Angular basis of centre type I against neighbour pair block (J,K) (BasisA,
+// src/nnp/basis_angular.hpp:53-115), GAUSS form.  The block's functions are mapped onto a
+// grid (distinct 1/eta^alpha) x (distinct lambda) x (zeta = 2^m); gidx[f] is the grid cell
+// (e*NL + l)*NZ_MAX + m of file function f.
+struct AngP {
+  int n, off, cut, alpha;
+  float rc, pirc, rci, norm;
+  int ne, nl, nz, pad;
+  float ietap[NE_MAX];
+  float lam[NL];
+  signed char gidx[NA_MAX];
+};
+
+struct PotParams {
+  int ntypes;
+  float rc;
+  int nin[NT_MAX];
+  RadialP rad[NT_MAX][NT_MAX];
+  AngP ang[NT_MAX][NB_MAX];
+};
+
+__host__ __device__ inline int lidx(int i, int j) { return (i >= j) ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
+
+// One atomic network on the device (NN::ANN, src/ml/nn.hpp:218-341).  Weights are row-major
+// [out][in] (as ANN::w_), plus a transposed copy [in][out] for the forward GEMMs.
+struct NetP {
+  int nin, nlayer, act, pad;
+  int nodes[NLAYER_MAX];
+  const float* w[NLAYER_MAX];   // [nodes[l]][cols(l)]
+  const float* wt[NLAYER_MAX];  // [cols(l)][nodes[l]]
+  const float* b[NLAYER_MAX];
+  const float* inpw;
+  const float* inpb;
+  float outw, outb;
+  double evac;  // species vacuum energy (Type::energy, src/nnp/type.hpp)
+};
+struct NetsP {
+  NetP net[NT_MAX];
+};
+
+// Per-structure geometry of a batch.  mode: 0 non-periodic, 1 image shells (some shell > 0),
+// 2 single image (all shells 0: at most one image of each atom within the cutoff).
+struct StrucMeta {
+  int atom0, natoms, mode, nimg;
+  int img0, pad0, pad1, pad2;
+  double R[9], RInv[9];  // column-major
+  double dMax2, fro;
+  double shifts[18];     // +col0, -col0, +col1, -col1, +col2, -col2 (Cell::init, src/struc/cell.cpp:63-69)
+  float Rf[9];
+  float margin;          // FP32 filter margin on r^2
+};
+// One lattice shift of the image box, in the reference's enumeration order.
+struct ImgEntry {
+  double v[3];
+  int n[3];
+  int pad;
+};
+
+// Device status words (one int array per context).
+enum { ST_MAXCOUNT = 0, ST_ORPHANS = 1, ST_ERROR = 2, ST_WORDS = 8 };
+enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_ORPHANS = 4 };
+
+#ifdef __CUDACC__
+// ---- exact FP64 helpers: fixed evaluation order and no FMA contraction, so that the GPU
+// reproduces the oracle's (and the reference's) rounding of Cell::diff and |r|^2 bit for bit.
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double sqn3(double x, double y, double z) { return dadd(dadd(dmul(x, x), dmul(y, y)), dmul(z, z)); }
+// o = M v, M column-major, summed in index order
+__device__ __forceinline__ void matvec(const double* M, double v0, double v1, double v2, double& o0, double& o1, double& o2) {
+  o0 = dadd(dadd(dmul(M[0], v0), dmul(M[3], v1)), dmul(M[6], v2));
+  o1 = dadd(dadd(dmul(M[1], v0), dmul(M[4], v1)), dmul(M[7], v2));
+  o2 = dadd(dadd(dmul(M[2], v0), dmul(M[5], v1)), dmul(M[8], v2));
+}
+// math::special::mod(n,-0.5,0.5) (src/math/special.hpp:43-46); fmod(x,1) == x - trunc(x) exactly.
+__device__ __forceinline__ double modhalf(double n) {
+  const double x = dsub(n, -0.5);
+  const double a = dsub(x, trunc(x));
+  const double b = dadd(a, 1.0);
+  const double c = dsub(b, trunc(b));
+  return dadd(c, -0.5);
+}
+// Cell::diff (src/struc/cell.cpp:103-128): minimum-image difference p1-p2 with the 6-shift
+// fallback; D receives the integer translation (diff = p1 - p2 - R*D).
+__device__ __forceinline__ void cell_diff(const StrucMeta& S, double p0, double p1, double p2, double q0, double q1, double q2,
+                                          double& o0, double& o1, double& o2, int D[3]) {
+  double f0, f1, f2;
+  matvec(S.RInv, dsub(p0, q0), dsub(p1, q1), dsub(p2, q2), f0, f1, f2);
+  const double m0 = modhalf(f0), m1 = modhalf(f1), m2 = modhalf(f2);
+  D[0] = (int)llrint(f0 - m0);
+  D[1] = (int)llrint(f1 - m1);
+  D[2] = (int)llrint(f2 - m2);
+  matvec(S.R, m0, m1, m2, o0, o1, o2);
+  if (sqn3(o0, o1, o2) > S.dMax2) {
+    double dmin2 = sqn3(o0, o1, o2), r0 = o0, r1 = o1, r2 = o2;
+    int best = -1;
+    for (int k = 0; k < 6; ++k) {
+      const double t0 = dadd(o0, S.shifts[3 * k]), t1 = dadd(o1, S.shifts[3 * k + 1]), t2 = dadd(o2, S.shifts[3 * k + 2]);
+      const double d2 = sqn3(t0, t1, t2);
+      if (d2 < dmin2) { dmin2 = d2; r0 = t0; r1 = t1; r2 = t2; best = k; }
+    }
+    if (best >= 0) D[best / 2] += (best % 2 == 0) ? -1 : 1;
+    o0 = r0; o1 = r1; o2 = r2;
+  }
+}
+
+#endif  // __CUDACC__
+
+// Neighbour slot code: bits 0-23 hold the lattice translation (3 x signed 8 bit), bit 24 the
+// minimum-image flag.
+__host__ __device__ inline int pack_code(int t0, int t1, int t2, bool mn) {
+  return ((t0 + 128) & 0xff) | (((t1 + 128) & 0xff) << 8) | (((t2 + 128) & 0xff) << 16) | (mn ? (1 << 24) : 0);
+}
+__host__ __device__ inline bool code_min(int c) { return (c >> 24) & 1; }
+__host__ __device__ inline int code_t(int c, int k) { return ((c >> (8 * k)) & 0xff) - 128; }
+
+#ifdef __CUDACC__
+// ---- cutoff functions (Basis::cut_func / cut_grad, src/nnp/basis.cpp:80-120), FP32
+__device__ __forceinline__ void cutoff_fg(int cut, float d, float rc, float pirc, float rci, float& f, float& g) {
+  if (cut == CUT_COS) {
+    if (d < rc) {
+      float s, c;
+      sincosf(d * pirc, &s, &c);
+      f = 0.5f * (c + 1.0f);
+      g = -0.5f * pirc * s;
+    } else {
+      f = (d > rc) ? 0.f : 0.5f * (cosf(d * pirc) + 1.0f);
+      g = 0.f;
+    }
+  } else if (cut == CUT_TANH) {
+    const float t = (d > rc) ? 0.f : tanhf(1.0f - d * rci);
+    f = t * t * t;
+    g = (d < rc) ? -3.0f * t * t * (1.0f - t * t) * rci : 0.f;
+  } else {  // STEP
+    f = (d > rc) ? 0.f : 1.f;
+    g = 0.f;
+  }
+}
+
+// species index clamped into the table (invalid input is flagged by frac_kernel)
+__device__ __forceinline__ int clamp_type(int t, int ntypes) { return t < 0 ? 0 : (t >= ntypes ? ntypes - 1 : t); }
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+#endif  // __CUDACC__
+
+}  // namespace nnpgpu

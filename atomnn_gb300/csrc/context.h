@@ -1,0 +1,73 @@
+// context.h - the engine context behind the C ABI (include/nnpgpu.h).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/nnpgpu.h"
+#include "kernels.h"
+#include "potential.h"
+#include "serve.h"
+
+namespace nnpgpu {
+
+// A device buffer that grows on demand and counts against the context's HBM budget.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+// Host-side geometry of one structure (mirrors Cell::init and the shell set-up of
+// NeighborList::build, src/struc/cell.cpp:45-70 and src/struc/neighbor.cpp:67-95).
+void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& m, std::vector<ImgEntry>& imgs);
+
+class Serving;
+
+}  // namespace nnpgpu
+
+struct nnpgpu_ctx {
+  std::string err;
+  int device = 0;
+  int verbose = 0;
+  cudaStream_t stream = nullptr;
+  nnpgpu::HPot pot;
+  nnpgpu::PotParams P;
+  int ne = 1, nz = 1, max_nin = 0, gstride = 0;
+  nnpgpu::NetsP nets{};
+  void* netbuf = nullptr;
+  size_t netbytes = 0;
+  void* tcbuf = nullptr;  // BF16 weights of the tensor-core path
+  size_t tcbytes = 0;
+  size_t budget = 0, used = 0;
+  int cap_hint = 0;
+  nnpgpu::TuneCfg tune;
+  // batch buffers
+  nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, nb_j, nb_r, nb_code, nb_cnt, nb_rev, orphans, G, dEdG, eatom, perm,
+      type_count, W, force, energy, status;
+  nnpgpu::HostBuf h_meta, h_in, h_out;  // pinned staging: geometry, inputs, outputs
+  int buf_generation = 0;
+  // captured launch sequences of the batched path, keyed by batch shape
+  typedef std::tuple<int, int, int, int, int, const void*, const void*, const void*, const void*> GraphKey;
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  std::map<GraphKey, int> shapes_seen;
+  std::unique_ptr<nnpgpu::Serving> serving;
+};
+
+namespace nnpgpu {
+// Grow dev to at least bytes (never shrinks).  Returns false on allocation failure / budget.
+bool ensure(nnpgpu_ctx* c, DevBuf& b, size_t bytes);
+bool ensure_host(nnpgpu_ctx* c, HostBuf& b, size_t bytes);
+// Runs the launch sequence for atoms of structures [s0, s0+ns) of the uploaded batch.
+int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st);
+int set_error(nnpgpu_ctx* c, int code, const std::string& msg);
+// Packs the BF16 weights of the tensor-core network path (network_tc.cu).
+int prepare_tc_weights(nnpgpu_ctx* c);
+}  // namespace nnpgpu

@@ -1,0 +1,101 @@
+// gather.cu - force assembly and per-structure energy.
+//
+// NNP::force (src/nnp/nnp.cpp:416-482) adds each neighbour-slot contribution W to the centre
+// atom and subtracts it from the neighbour only when the slot is the neighbour's minimum image.
+// Here F_j = sum_{s in list(j)} W[j,s] - sum_{s in list(j), min} W[rev(j,s)], where rev is the
+// transposed slot built by reverse_kernel: a gather over the atom's own list, FP64, no atomics.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace nnpgpu {
+
+__global__ void __launch_bounds__(128) gather_kernel(int a0, int natoms, int cap, const int* __restrict__ nb_code,
+                                                     const int* __restrict__ nb_cnt, const int* __restrict__ nb_rev,
+                                                     const float4* __restrict__ W, double* __restrict__ force) {
+  const int lane = threadIdx.x & 31;
+  const int j = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (j >= a0 + natoms) return;
+  const int n = min(nb_cnt[j], cap);
+  double fx = 0, fy = 0, fz = 0;
+  for (int s = lane; s < n; s += 32) {
+    const size_t g = (size_t)j * cap + s;
+    const float4 w = W[g];
+    fx += w.x;
+    fy += w.y;
+    fz += w.z;
+    if (code_min(nb_code[g])) {
+      const int r = nb_rev[g];
+      if (r >= 0) {
+        const float4 v = W[r];
+        fx -= v.x;
+        fy -= v.y;
+        fz -= v.z;
+      }
+    }
+  }
+  fx = warp_sum_d(fx);
+  fy = warp_sum_d(fy);
+  fz = warp_sum_d(fz);
+  if (lane == 0) {
+    force[3 * (size_t)j] = fx;
+    force[3 * (size_t)j + 1] = fy;
+    force[3 * (size_t)j + 2] = fz;
+  }
+}
+
+// Sources whose transposed slot could not be matched: subtract serially (deterministic order).
+__global__ void orphan_kernel(int cap, const int* __restrict__ nb_j, const float4* __restrict__ W, const int* __restrict__ orphans,
+                              int* __restrict__ status, int orphan_cap, double* __restrict__ force) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int n = min(status[ST_ORPHANS], orphan_cap);
+  if (n > 4096) {  // far more than rounding ties can produce: report instead of a long serial pass
+    atomicOr(&status[ST_ERROR], ERR_ORPHANS);
+    return;
+  }
+  // insertion order from atomics is arbitrary: apply in increasing slot order
+  int last = -1;
+  for (int k = 0; k < n; ++k) {
+    int best = 0x7fffffff;
+    for (int q = 0; q < n; ++q)
+      if (orphans[q] > last && orphans[q] < best) best = orphans[q];
+    last = best;
+    const int j = nb_j[best];
+    const float4 v = W[best];
+    force[3 * (size_t)j] -= v.x;
+    force[3 * (size_t)j + 1] -= v.y;
+    force[3 * (size_t)j + 2] -= v.z;
+  }
+}
+
+// One CTA per structure: E = sum_i NN_i (+ vacuum energy of each atom's species), FP64.
+__global__ void __launch_bounds__(256) energy_kernel(int s0, int ntypes, const StrucMeta* __restrict__ meta, const int* __restrict__ type,
+                                                     const float* __restrict__ eatom, const __grid_constant__ NetsP N,
+                                                     int add_vacuum, double* __restrict__ energy) {
+  __shared__ double red[8];
+  const StrucMeta& S = meta[s0 + blockIdx.x];
+  double e = 0;
+  for (int a = threadIdx.x; a < S.natoms; a += blockDim.x) {
+    const int i = S.atom0 + a;
+    e += (double)eatom[i];
+    if (add_vacuum) e += N.net[clamp_type(type[i], ntypes)].evac;
+  }
+  e = warp_sum_d(e);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    energy[s0 + blockIdx.x] = t;
+  }
+}
+
+void launch_gather(const BatchDev& B, const NetsP& N, bool add_vacuum, bool want_force, cudaStream_t st) {
+  if (B.natoms == 0) return;
+  if (want_force) {
+    gather_kernel<<<(B.natoms + 3) / 4, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.nb_code, B.nb_cnt, B.nb_rev, B.W, B.force);
+    orphan_kernel<<<1, 32, 0, st>>>(B.cap, B.nb_j, B.W, B.orphans, B.status, B.orphan_cap, B.force);
+  }
+  energy_kernel<<<B.nstruc, 256, 0, st>>>(B.s0, B.ntypes, B.meta, B.type, B.eatom, N, add_vacuum ? 1 : 0, B.energy);
+}
+
+}  // namespace nnpgpu

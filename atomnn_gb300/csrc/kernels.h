@@ -1,0 +1,67 @@
+// kernels.h - device buffers of one batch and the kernel launchers (host-side interface).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace nnpgpu {
+
+// All device pointers of one batch of structures.  Atoms of a structure are contiguous;
+// per-atom neighbour data uses fixed-stride slots [i*cap, i*cap+cap).
+struct BatchDev {
+  int natoms = 0, nstruc = 0, cap = 0;
+  int a0 = 0, s0 = 0;
+  int ntypes = 1;  // first atom / structure of this view (all arrays are batch-indexed)
+  double rc = 0;
+  // inputs
+  const double* posn = nullptr;  // [natoms*3]
+  const int* type = nullptr;     // [natoms]
+  const int* atom_struc = nullptr;
+  const StrucMeta* meta = nullptr;
+  const ImgEntry* imgs = nullptr;
+  // neighbour lists
+  float4* sfrac = nullptr;
+  int* nb_j = nullptr;
+  float4* nb_r = nullptr;
+  int* nb_code = nullptr;
+  int* nb_cnt = nullptr;
+  int* nb_rev = nullptr;
+  int* orphans = nullptr;
+  int orphan_cap = 0;
+  // descriptors and networks
+  float* G = nullptr;      // [natoms*gstride]
+  float* dEdG = nullptr;   // [natoms*gstride]
+  int gstride = 0;
+  float* eatom = nullptr;  // [natoms] network output
+  int* perm = nullptr;     // [natoms] atoms grouped by type
+  int* type_count = nullptr;  // [NT_MAX+1] counters (device)
+  // forces
+  float4* W = nullptr;     // [natoms*cap] per-slot gradient contribution
+  double* force = nullptr; // [natoms*3] output
+  double* energy = nullptr;  // [nstruc] output
+  int* status = nullptr;   // [ST_WORDS]
+};
+
+// Launch configuration chosen by the autotuner (atoms per CTA for the triplet kernels).
+struct TuneCfg {
+  int warps_symm = 4;
+  int warps_force = 4;
+  int nn_tile = 32;
+};
+
+void launch_neighbors(const BatchDev& B, cudaStream_t st);
+void launch_reverse(const BatchDev& B, cudaStream_t st);
+// descriptors (NNP::symm) and chain rule (NNP::force) ; ne/nz select the template instance
+int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
+int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
+size_t symm_smem_bytes(int cap, int ne, int warps);
+size_t force_smem_bytes(int cap, int ne, int warps);
+// atomic networks: FP32 SIMT path and BF16 tensor-core path
+void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st);
+void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile, cudaStream_t st);
+int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weights, int ntypes, cudaStream_t st);
+// force gather, orphan fix-up, per-structure energy
+void launch_gather(const BatchDev& B, const NetsP& N, bool add_vacuum, bool want_force, cudaStream_t st);
+
+}  // namespace nnpgpu

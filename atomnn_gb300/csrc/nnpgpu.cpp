@@ -1,0 +1,589 @@
+// nnpgpu.cpp - the C ABI (include/nnpgpu.h): context, batch set-up and the launch sequence.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+
+#include "context.h"
+
+using namespace nnpgpu;
+
+namespace nnpgpu {
+
+int set_error(nnpgpu_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+static int cuda_fail(nnpgpu_ctx* c, cudaError_t e, const char* where) {
+  return set_error(c, NNPGPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+bool ensure(nnpgpu_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes <= b.bytes) return true;
+  size_t want = std::max(bytes, b.bytes + b.bytes / 2);
+  want = (want + 255) & ~(size_t)255;
+  if (c->budget && c->used - b.bytes + want > c->budget) {
+    want = bytes;
+    if (c->used - b.bytes + want > c->budget) return false;
+  }
+  if (b.p) cudaFree(b.p);
+  c->used -= b.bytes;
+  b.p = nullptr;
+  b.bytes = 0;
+  if (cudaMalloc(&b.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  b.bytes = want;
+  c->used += want;
+  c->buf_generation++;
+  return true;
+}
+
+bool ensure_host(nnpgpu_ctx* c, HostBuf& b, size_t bytes) {
+  (void)c;
+  if (bytes <= b.bytes) return true;
+  size_t want = std::max(bytes, b.bytes + b.bytes / 2);
+  if (b.p) cudaFreeHost(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  if (cudaMallocHost(&b.p, want) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  b.bytes = want;
+  return true;
+}
+
+static double nrm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
+
+void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& m, std::vector<ImgEntry>& imgs) {
+  std::memset(&m, 0, sizeof(m));
+  m.atom0 = atom0;
+  m.natoms = natoms;
+  double fro = 0;
+  for (int k = 0; k < 9; ++k) {
+    m.R[k] = cell ? cell[k] : 0.0;
+    fro += m.R[k] * m.R[k];
+  }
+  fro = std::sqrt(fro);
+  m.fro = fro;
+  if (!(fro > 0)) {
+    m.mode = 0;
+    return;
+  }
+  auto M = [&](int r, int c) { return m.R[3 * c + r]; };
+  // inverse by cofactors (Cell::init, src/struc/cell.cpp:49)
+  const double c00 = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+  const double c01 = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
+  const double c02 = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+  const double det = M(0, 0) * c00 + M(0, 1) * c01 + M(0, 2) * c02;
+  if (det == 0 || !std::isfinite(det)) throw PotError(NNPGPU_ERR_INVALID, "singular or non-finite cell");
+  const double id = 1.0 / det;
+  double inv[3][3];
+  inv[0][0] = c00 * id;
+  inv[1][0] = c01 * id;
+  inv[2][0] = c02 * id;
+  inv[0][1] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) * id;
+  inv[1][1] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) * id;
+  inv[2][1] = (M(0, 1) * M(2, 0) - M(0, 0) * M(2, 1)) * id;
+  inv[0][2] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) * id;
+  inv[1][2] = (M(0, 2) * M(1, 0) - M(0, 0) * M(1, 2)) * id;
+  inv[2][2] = (M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0)) * id;
+  for (int r = 0; r < 3; ++r)
+    for (int c = 0; c < 3; ++c) m.RInv[3 * c + r] = inv[r][c];
+  double col[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) col[c][r] = m.R[3 * c + r];
+  double dmax = nrm3(col[0]);
+  for (int c = 1; c < 3; ++c) dmax = std::min(dmax, nrm3(col[c]));
+  dmax *= 0.5;
+  m.dMax2 = dmax * dmax;
+  for (int c = 0; c < 3; ++c)
+    for (int r = 0; r < 3; ++r) {
+      m.shifts[6 * c + r] = col[c][r];
+      m.shifts[6 * c + 3 + r] = -col[c][r];
+    }
+  for (int k = 0; k < 9; ++k) m.Rf[k] = (float)m.R[k];
+  // image shells (NeighborList::build, src/struc/neighbor.cpp:70-95), lattice vectors sorted
+  // by decreasing norm with a stable order for ties
+  int perm[3] = {0, 1, 2};
+  std::stable_sort(perm, perm + 3, [&](int a, int b) { return nrm3(col[a]) > nrm3(col[b]); });
+  const double* R0 = col[perm[0]];
+  const double* R1 = col[perm[1]];
+  const double* R2 = col[perm[2]];
+  const double cx[3] = {R0[1] * R1[2] - R0[2] * R1[1], R0[2] * R1[0] - R0[0] * R1[2], R0[0] * R1[1] - R0[1] * R1[0]};
+  const double dot2 = R2[0] * cx[0] + R2[1] * cx[1] + R2[2] * cx[2];
+  int shell[3];
+  shell[0] = (int)std::floor(2.0 * rc / nrm3(R0));
+  shell[1] = (int)std::floor(2.0 * rc / (nrm3(cx) / nrm3(R0)));
+  shell[2] = (int)std::floor(2.0 * rc / std::fabs(dot2 / (nrm3(R0) * nrm3(R1))));
+  double Lsum = nrm3(col[0]) + nrm3(col[1]) + nrm3(col[2]);
+  m.margin = (float)(2.0 * rc * (Lsum * 1e-6 + 1e-5) + 1e-4 * rc * rc);
+  if (shell[0] == 0 && shell[1] == 0 && shell[2] == 0) {
+    m.mode = 2;
+    return;
+  }
+  m.mode = 1;
+  m.img0 = (int)imgs.size();
+  for (int i = -shell[0]; i <= shell[0]; ++i)
+    for (int j = -shell[1]; j <= shell[1]; ++j)
+      for (int k = -shell[2]; k <= shell[2]; ++k) {
+        ImgEntry e;
+        std::memset(&e, 0, sizeof(e));
+        for (int x = 0; x < 3; ++x) e.v[x] = i * R0[x] + j * R1[x] + k * R2[x];
+        e.n[perm[0]] = i;
+        e.n[perm[1]] = j;
+        e.n[perm[2]] = k;
+        imgs.push_back(e);
+      }
+  m.nimg = (int)imgs.size() - m.img0;
+}
+
+// Neighbour capacity estimate from the densest structure (rounded up to 32).
+static int estimate_cap(const nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell) {
+  double best = 16;
+  const double rc = c->pot.rc;
+  for (int s = 0; s < nstruc; ++s) {
+    const double* R = cell + 9 * s;
+    const double vol = std::fabs(R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]));
+    double nb;
+    if (vol > 0) nb = natoms[s] / vol * 4.0 / 3.0 * M_PI * std::pow(rc + 0.5, 3) * 1.25 + 16;
+    else nb = natoms[s];
+    best = std::max(best, nb);
+  }
+  int cap = (int)std::ceil(best / 32.0) * 32;
+  if (c->cap_hint > 0) cap = std::max(cap, c->cap_hint);
+  return std::min(cap, 256);
+}
+
+int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
+  const bool want_force = flags & NNPGPU_FORCE;
+  const bool want_energy = flags & NNPGPU_ENERGY;
+  launch_neighbors(B, st);
+  if (want_force) launch_reverse(B, st);
+  if (launch_symm(B, c->P, c->ne, c->nz, c->tune.warps_symm, st) != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "no symm kernel instance");
+  if (want_energy || want_force) {
+    launch_type_sort(B, c->pot.ntypes, st);
+    if (flags & NNPGPU_BF16) {
+      const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st);
+      if (rcode != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "BF16 network path unavailable for this potential");
+    } else {
+      launch_network_fp32(B, c->nets, c->pot.ntypes, c->tune.nn_tile, st);
+    }
+    if (want_force)
+      if (launch_force(B, c->P, c->ne, c->nz, c->tune.warps_force, st) != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "no force kernel instance");
+    launch_gather(B, c->nets, !(flags & NNPGPU_NO_VACUUM), want_force, st);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
+  return NNPGPU_OK;
+}
+
+}  // namespace nnpgpu
+
+// ------------------------------------------------------------------------------------------
+namespace {
+
+struct Uploaded {
+  int natoms = 0, nstruc = 0, cap = 0;
+  std::vector<StrucMeta> metas;
+  std::vector<int> offsets;
+};
+
+// Validates the batch description and uploads geometry metadata; sizes all batch buffers.
+int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, int cap, Uploaded& U, cudaStream_t st) {
+  if (nstruc < 0 || (nstruc > 0 && (!natoms || !cell))) return set_error(c, NNPGPU_ERR_INVALID, "invalid batch description");
+  U.nstruc = nstruc;
+  U.offsets.assign(nstruc + 1, 0);
+  for (int s = 0; s < nstruc; ++s) {
+    if (natoms[s] < 0) return set_error(c, NNPGPU_ERR_INVALID, "negative atom count");
+    U.offsets[s + 1] = U.offsets[s] + natoms[s];
+  }
+  U.natoms = U.offsets[nstruc];
+  std::vector<ImgEntry> imgs;
+  U.metas.resize(nstruc);
+  try {
+    for (int s = 0; s < nstruc; ++s) make_meta(cell + 9 * s, U.offsets[s], natoms[s], c->pot.rc, U.metas[s], imgs);
+  } catch (PotError& e) {
+    return set_error(c, e.code, e.what());
+  }
+  if (imgs.empty()) imgs.resize(1);
+  U.cap = cap;
+  const size_t N = std::max(U.natoms, 1);
+  const size_t NC = N * cap;
+  bool ok = true;
+  ok = ok && ensure(c, c->posn, sizeof(double) * 3 * N) && ensure(c, c->type, sizeof(int) * N) &&
+       ensure(c, c->atom_struc, sizeof(int) * N) && ensure(c, c->meta, sizeof(StrucMeta) * std::max(nstruc, 1)) &&
+       ensure(c, c->imgs, sizeof(ImgEntry) * imgs.size()) && ensure(c, c->sfrac, sizeof(float4) * N) &&
+       ensure(c, c->nb_j, sizeof(int) * NC) && ensure(c, c->nb_r, sizeof(float4) * NC) && ensure(c, c->nb_code, sizeof(int) * NC) &&
+       ensure(c, c->nb_cnt, sizeof(int) * N) && ensure(c, c->nb_rev, sizeof(int) * NC) && ensure(c, c->orphans, sizeof(int) * N) &&
+       ensure(c, c->G, sizeof(float) * N * c->gstride) && ensure(c, c->dEdG, sizeof(float) * N * c->gstride) &&
+       ensure(c, c->eatom, sizeof(float) * N) && ensure(c, c->perm, sizeof(int) * N) &&
+       ensure(c, c->type_count, sizeof(int) * (3 * NT_MAX + 3)) && ensure(c, c->W, sizeof(float4) * NC) &&
+       ensure(c, c->force, sizeof(double) * 3 * N) && ensure(c, c->energy, sizeof(double) * std::max(nstruc, 1)) &&
+       ensure(c, c->status, sizeof(int) * ST_WORDS);
+  if (!ok) return set_error(c, NNPGPU_ERR_OOM, "device allocation failed or HBM budget exceeded");
+  // atom -> structure map and metadata
+  std::vector<int> as(N, 0);
+  for (int s = 0; s < nstruc; ++s)
+    for (int a = U.offsets[s]; a < U.offsets[s + 1]; ++a) as[a] = s;
+  const size_t meta_bytes = sizeof(StrucMeta) * nstruc, img_bytes = sizeof(ImgEntry) * imgs.size(), as_bytes = sizeof(int) * N;
+  cudaStreamSynchronize(st);  // the staging buffer may still feed an earlier copy
+  if (!ensure_host(c, c->h_meta, meta_bytes + img_bytes + as_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
+  char* h = (char*)c->h_meta.p;
+  std::memcpy(h, U.metas.data(), meta_bytes);
+  std::memcpy(h + meta_bytes, imgs.data(), img_bytes);
+  std::memcpy(h + meta_bytes + img_bytes, as.data(), as_bytes);
+  cudaMemcpyAsync(c->meta.p, h, meta_bytes, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->imgs.p, h + meta_bytes, img_bytes, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->atom_struc.p, h + meta_bytes + img_bytes, as_bytes, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(c->status.p, 0, sizeof(int) * ST_WORDS, st);
+  return NNPGPU_OK;
+}
+
+BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const int* type, double* energy, double* force) {
+  BatchDev B;
+  B.natoms = U.natoms;
+  B.nstruc = U.nstruc;
+  B.cap = U.cap;
+  B.rc = c->pot.rc;
+  B.ntypes = c->pot.ntypes;
+  B.posn = posn;
+  B.type = type;
+  B.atom_struc = (const int*)c->atom_struc.p;
+  B.meta = (const StrucMeta*)c->meta.p;
+  B.imgs = (const ImgEntry*)c->imgs.p;
+  B.sfrac = (float4*)c->sfrac.p;
+  B.nb_j = (int*)c->nb_j.p;
+  B.nb_r = (float4*)c->nb_r.p;
+  B.nb_code = (int*)c->nb_code.p;
+  B.nb_cnt = (int*)c->nb_cnt.p;
+  B.nb_rev = (int*)c->nb_rev.p;
+  B.orphans = (int*)c->orphans.p;
+  B.orphan_cap = std::max(U.natoms, 1);
+  B.G = (float*)c->G.p;
+  B.dEdG = (float*)c->dEdG.p;
+  B.gstride = c->gstride;
+  B.eatom = (float*)c->eatom.p;
+  B.perm = (int*)c->perm.p;
+  B.type_count = (int*)c->type_count.p;
+  B.W = (float4*)c->W.p;
+  B.force = force;
+  B.energy = energy;
+  B.status = (int*)c->status.p;
+  return B;
+}
+
+// Enqueues the pipeline for the whole batch (batched) or one structure at a time (plain).
+int enqueue(nnpgpu_ctx* c, const Uploaded& U, const BatchDev& Ball, int flags, cudaStream_t st) {
+  if (flags & NNPGPU_BATCHED) {
+    const nnpgpu_ctx::GraphKey key(U.natoms, U.nstruc, U.cap, flags, c->buf_generation, Ball.posn, Ball.type, Ball.energy, Ball.force);
+    auto it = c->graphs.find(key);
+    if (it != c->graphs.end()) {
+      const cudaError_t e = cudaGraphLaunch(it->second, st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "cudaGraphLaunch");
+      return NNPGPU_OK;
+    }
+    // first run of a shape is a plain launch sequence; the second one is captured
+    if (c->shapes_seen[key]++ == 0) return run_pipeline(c, Ball, flags, st);
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return cuda_fail(c, cudaGetLastError(), "capture");
+    const int rc = run_pipeline(c, Ball, flags, st);
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != NNPGPU_OK) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) return cuda_fail(c, e, "cudaStreamEndCapture");
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t e2 = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return cuda_fail(c, e2, "cudaGraphInstantiate");
+    c->graphs[key] = ex;
+    const cudaError_t e3 = cudaGraphLaunch(ex, st);
+    if (e3 != cudaSuccess) return cuda_fail(c, e3, "cudaGraphLaunch");
+    return NNPGPU_OK;
+  }
+  for (int s = 0; s < U.nstruc; ++s) {
+    BatchDev B = Ball;
+    B.a0 = U.offsets[s];
+    B.natoms = U.offsets[s + 1] - U.offsets[s];
+    B.s0 = s;
+    B.nstruc = 1;
+    const int rc = run_pipeline(c, B, flags, st);
+    if (rc != NNPGPU_OK) return rc;
+  }
+  return NNPGPU_OK;
+}
+
+void drop_graphs(nnpgpu_ctx* c) {
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+  c->graphs.clear();
+}
+
+// Reads the status words after the stream finished; returns OK, a retry request (>0 = new
+// capacity) or an error.
+int check_status(nnpgpu_ctx* c, const int* st_words, int cap) {
+  if (st_words[ST_ERROR] & ERR_BAD_POSITION) return set_error(c, NNPGPU_ERR_INVALID, "non-finite atom position");
+  if (st_words[ST_ERROR] & ERR_BAD_TYPE) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
+  if (st_words[ST_ERROR] & ERR_ORPHANS) return set_error(c, NNPGPU_ERR_INVALID, "inconsistent neighbour lists (too many unmatched minimum images)");
+  if (st_words[ST_MAXCOUNT] > cap) {
+    const int need = (st_words[ST_MAXCOUNT] + 31) / 32 * 32;
+    if (need > 256) return set_error(c, NNPGPU_ERR_CAPACITY, "more than 256 neighbours within the cutoff for some atom");
+    return need;
+  }
+  return 0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------ C ABI
+extern "C" int nnpgpu_create(const char* potfile, const nnpgpu_opts* opts, nnpgpu_ctx** out) {
+  if (!out) return NNPGPU_ERR_INVALID;
+  *out = nullptr;
+  nnpgpu_ctx* c = new nnpgpu_ctx();
+  try {
+    c->device = opts ? opts->device : 0;
+    c->verbose = opts ? opts->verbose : 0;
+    c->budget = opts ? opts->hbm_budget_bytes : 0;
+    c->cap_hint = opts ? opts->max_neighbors : 0;
+    if (!potfile) throw PotError(NNPGPU_ERR_INVALID, "no potential file");
+    c->pot = read_potential(potfile);
+    build_tables(c->pot, c->P, c->ne, c->nz);
+    c->max_nin = 0;
+    for (int t = 0; t < c->pot.ntypes; ++t) c->max_nin = std::max(c->max_nin, c->pot.nin[t]);
+    c->gstride = (c->max_nin + 15) / 16 * 16;
+  } catch (PotError& e) {
+    const int code = e.code;
+    c->err = e.what();
+    *out = c;  // keep the context so that the caller can read the message
+    return code;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= c->device) {
+    cudaGetLastError();
+    *out = c;
+    return set_error(c, NNPGPU_ERR_CUDA, "no CUDA device available (the engine has no CPU fallback)");
+  }
+  cudaError_t e = cudaSetDevice(c->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    *out = c;
+    return cuda_fail(c, e, "device set-up");
+  }
+  // FP32 network weights: per type and layer w (row-major), wt (transposed), b, plus inpw/inpb
+  std::vector<float> host;
+  std::vector<size_t> offs;
+  auto push = [&](const std::vector<float>& v) {
+    while (host.size() % 4) host.push_back(0.f);
+    offs.push_back(host.size());
+    host.insert(host.end(), v.begin(), v.end());
+  };
+  for (int t = 0; t < c->pot.ntypes; ++t) {
+    const HNet& n = c->pot.nets[t];
+    const int L = (int)n.nodes.size();
+    for (int l = 0; l < L; ++l) {
+      const int R = n.nodes[l], C = l == 0 ? n.nin : n.nodes[l - 1];
+      std::vector<float> w(n.w[l].begin(), n.w[l].end()), wt((size_t)R * C), b(n.b[l].begin(), n.b[l].end());
+      for (int r = 0; r < R; ++r)
+        for (int q = 0; q < C; ++q) wt[(size_t)q * R + r] = (float)n.w[l][(size_t)r * C + q];
+      push(w);
+      push(wt);
+      push(b);
+    }
+    push(std::vector<float>(n.inpw.begin(), n.inpw.end()));
+    push(std::vector<float>(n.inpb.begin(), n.inpb.end()));
+  }
+  c->netbytes = host.size() * sizeof(float);
+  if (cudaMalloc(&c->netbuf, c->netbytes) != cudaSuccess) {
+    cudaGetLastError();
+    *out = c;
+    return set_error(c, NNPGPU_ERR_OOM, "could not allocate network weights");
+  }
+  c->used += c->netbytes;
+  cudaMemcpy(c->netbuf, host.data(), c->netbytes, cudaMemcpyHostToDevice);
+  size_t k = 0;
+  const float* base = (const float*)c->netbuf;
+  for (int t = 0; t < c->pot.ntypes; ++t) {
+    const HNet& n = c->pot.nets[t];
+    NetP& p = c->nets.net[t];
+    p.nin = n.nin;
+    p.nlayer = (int)n.nodes.size();
+    p.act = n.act;
+    for (int l = 0; l < p.nlayer; ++l) {
+      p.nodes[l] = n.nodes[l];
+      p.w[l] = base + offs[k++];
+      p.wt[l] = base + offs[k++];
+      p.b[l] = base + offs[k++];
+    }
+    p.inpw = base + offs[k++];
+    p.inpb = base + offs[k++];
+    p.outw = (float)n.outw[0];
+    p.outb = (float)n.outb[0];
+    p.evac = c->pot.types[t].energy;
+  }
+  prepare_tc_weights(c);
+  *out = c;
+  return NNPGPU_OK;
+}
+
+extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
+  if (!c) return;
+  c->serving.reset();
+  drop_graphs(c);
+  DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
+                    &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
+                    &c->status};
+  for (DevBuf* b : bufs)
+    if (b->p) cudaFree(b->p);
+  if (c->netbuf) cudaFree(c->netbuf);
+  if (c->tcbuf) cudaFree(c->tcbuf);
+  if (c->h_meta.p) cudaFreeHost(c->h_meta.p);
+  if (c->h_in.p) cudaFreeHost(c->h_in.p);
+  if (c->h_out.p) cudaFreeHost(c->h_out.p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+extern "C" const char* nnpgpu_last_error(const nnpgpu_ctx* c) { return c ? c->err.c_str() : "no context"; }
+extern "C" int nnpgpu_ntypes(const nnpgpu_ctx* c) { return c ? c->pot.ntypes : 0; }
+extern "C" int nnpgpu_type_index(const nnpgpu_ctx* c, const char* name) {
+  if (!c || !name) return -1;
+  auto it = c->pot.index.find(name);
+  return it == c->pot.index.end() ? -1 : it->second;
+}
+extern "C" double nnpgpu_cutoff(const nnpgpu_ctx* c) { return c ? c->pot.rc : 0.0; }
+extern "C" int nnpgpu_ninput(const nnpgpu_ctx* c, int type) {
+  if (!c || type < 0 || type >= c->pot.ntypes) return -1;
+  return c->pot.nin[type];
+}
+
+static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
+                        int flags, double* energy, double* force, float* symm, bool device_io, cudaStream_t st) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  cudaSetDevice(c->device);
+  if (!st) st = c->stream;
+  if ((flags & NNPGPU_ENERGY) && !energy) return set_error(c, NNPGPU_ERR_INVALID, "energy output missing");
+  if ((flags & NNPGPU_FORCE) && !force) return set_error(c, NNPGPU_ERR_INVALID, "force output missing");
+  if ((flags & NNPGPU_SYMM) && !symm) return set_error(c, NNPGPU_ERR_INVALID, "symm output missing");
+  int total = 0;
+  for (int s = 0; s < nstruc; ++s) total += natoms ? natoms[s] : 0;
+  if (total > 0 && (!posn || !species)) return set_error(c, NNPGPU_ERR_INVALID, "positions or species missing");
+  if (!device_io)
+    for (int a = 0; a < total; ++a)
+      if (species[a] < 0 || species[a] >= c->pot.ntypes) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
+  int cap = estimate_cap(c, nstruc, natoms, cell);
+  for (int attempt = 0; attempt < 4; ++attempt) {
+    Uploaded U;
+    int rc = prepare(c, nstruc, natoms, cell, cap, U, st);
+    if (rc != NNPGPU_OK) return rc;
+    const size_t N = total;
+    const double* dposn = posn;
+    const int* dtype = species;
+    if (!device_io) {
+      // stage inputs through pinned memory
+      const size_t in_bytes = sizeof(double) * 3 * N + sizeof(int) * N;
+      if (!ensure_host(c, c->h_in, in_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
+      char* h = (char*)c->h_in.p;
+      std::memcpy(h, posn, sizeof(double) * 3 * N);
+      std::memcpy(h + sizeof(double) * 3 * N, species, sizeof(int) * N);
+      cudaMemcpyAsync(c->posn.p, h, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(c->type.p, h + sizeof(double) * 3 * N, sizeof(int) * N, cudaMemcpyHostToDevice, st);
+      dposn = (const double*)c->posn.p;
+      dtype = (const int*)c->type.p;
+    }
+    double* denergy = device_io ? energy : (double*)c->energy.p;
+    double* dforce = (device_io && force) ? force : (double*)c->force.p;
+    BatchDev B = batch_view(c, U, dposn, dtype, denergy ? denergy : (double*)c->energy.p, dforce);
+    rc = enqueue(c, U, B, flags, st);
+    if (rc != NNPGPU_OK) return rc;
+    // outputs
+    int hstat[ST_WORDS];
+    if (!device_io) {
+      const size_t out_bytes = sizeof(double) * (nstruc + 3 * N) + sizeof(int) * ST_WORDS;
+      if (!ensure_host(c, c->h_out, out_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
+      char* h = (char*)c->h_out.p;
+      if (flags & NNPGPU_ENERGY) cudaMemcpyAsync(h, c->energy.p, sizeof(double) * nstruc, cudaMemcpyDeviceToHost, st);
+      if (flags & NNPGPU_FORCE) cudaMemcpyAsync(h + sizeof(double) * nstruc, c->force.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st);
+      cudaMemcpyAsync(h + sizeof(double) * (nstruc + 3 * N), c->status.p, sizeof(int) * ST_WORDS, cudaMemcpyDeviceToHost, st);
+      if (flags & NNPGPU_SYMM)
+        cudaMemcpy2DAsync(symm, sizeof(float) * c->max_nin, c->G.p, sizeof(float) * c->gstride, sizeof(float) * c->max_nin, N,
+                          cudaMemcpyDeviceToHost, st);
+      const cudaError_t e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return cuda_fail(c, e, "compute");
+      std::memcpy(hstat, h + sizeof(double) * (nstruc + 3 * N), sizeof(hstat));
+      const int need = check_status(c, hstat, U.cap);
+      if (need < 0) return need;
+      if (need > 0) { cap = need; c->cap_hint = std::max(c->cap_hint, need); continue; }
+      if (flags & NNPGPU_ENERGY) std::memcpy(energy, h, sizeof(double) * nstruc);
+      if (flags & NNPGPU_FORCE) std::memcpy(force, h + sizeof(double) * nstruc, sizeof(double) * 3 * N);
+      return NNPGPU_OK;
+    }
+    if (flags & NNPGPU_SYMM)
+      cudaMemcpy2DAsync(symm, sizeof(float) * c->max_nin, c->G.p, sizeof(float) * c->gstride, sizeof(float) * c->max_nin, N,
+                        cudaMemcpyDeviceToDevice, st);
+    cudaMemcpyAsync(hstat, c->status.p, sizeof(hstat), cudaMemcpyDeviceToHost, st);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(c, e, "compute");
+    const int need = check_status(c, hstat, U.cap);
+    if (need < 0) return need;
+    if (need > 0) { cap = need; c->cap_hint = std::max(c->cap_hint, need); continue; }
+    return NNPGPU_OK;
+  }
+  return set_error(c, NNPGPU_ERR_CAPACITY, "neighbour capacity retries exhausted");
+}
+
+extern "C" int nnpgpu_compute(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
+                              int flags, double* energy, double* force, float* symm) {
+  return compute_impl(c, nstruc, natoms, posn, species, cell, flags, energy, force, symm, false, nullptr);
+}
+
+extern "C" int nnpgpu_compute_device(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* d_posn, const int* d_species,
+                                     const double* cell, int flags, double* d_energy, double* d_force, float* d_symm, void* stream) {
+  return compute_impl(c, nstruc, natoms, d_posn, d_species, cell, flags, d_energy, d_force, d_symm, true, (cudaStream_t)stream);
+}
+
+extern "C" int nnpgpu_neighbors(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, int cap, int* count, int* index,
+                                float* r, unsigned char* mn, int* shift) {
+  if (!c || natoms < 0 || cap <= 0 || (natoms > 0 && (!posn || !count))) return set_error(c, NNPGPU_ERR_INVALID, "invalid arguments");
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  const double zero[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const double* cl = cell ? cell : zero;
+  const int dcap = std::min(256, std::max(cap, estimate_cap(c, 1, &natoms, cl)));
+  Uploaded U;
+  int rc = prepare(c, 1, &natoms, cl, (dcap + 31) / 32 * 32, U, st);
+  if (rc != NNPGPU_OK) return rc;
+  cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, st);
+  BatchDev B = batch_view(c, U, (const double*)c->posn.p, nullptr, (double*)c->energy.p, (double*)c->force.p);
+  launch_neighbors(B, st);
+  std::vector<int> hj((size_t)natoms * U.cap), hc((size_t)natoms * U.cap), hn(natoms);
+  std::vector<float4> hr((size_t)natoms * U.cap);
+  int hstat[ST_WORDS];
+  cudaMemcpyAsync(hj.data(), c->nb_j.p, sizeof(int) * hj.size(), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hc.data(), c->nb_code.p, sizeof(int) * hc.size(), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hr.data(), c->nb_r.p, sizeof(float4) * hr.size(), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hn.data(), c->nb_cnt.p, sizeof(int) * natoms, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hstat, c->status.p, sizeof(hstat), cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "neighbors");
+  if (hstat[ST_ERROR] & ERR_BAD_POSITION) return set_error(c, NNPGPU_ERR_INVALID, "non-finite atom position");
+  int status = NNPGPU_OK;
+  for (int i = 0; i < natoms; ++i) {
+    count[i] = hn[i];
+    if (hn[i] > cap) status = set_error(c, NNPGPU_ERR_CAPACITY, "neighbour list longer than cap");
+    const int n = std::min(std::min(hn[i], cap), U.cap);
+    for (int s = 0; s < n; ++s) {
+      const size_t src = (size_t)i * U.cap + s, dst = (size_t)i * cap + s;
+      if (index) index[dst] = hj[src];
+      if (r) { r[4 * dst] = hr[src].x; r[4 * dst + 1] = hr[src].y; r[4 * dst + 2] = hr[src].z; r[4 * dst + 3] = hr[src].w; }
+      if (mn) mn[dst] = code_min(hc[src]) ? 1 : 0;
+      if (shift) for (int x = 0; x < 3; ++x) shift[3 * dst + x] = code_t(hc[src], x);
+    }
+  }
+  if (status == NNPGPU_OK && hstat[ST_MAXCOUNT] > U.cap) status = set_error(c, NNPGPU_ERR_CAPACITY, "neighbour list longer than 256");
+  return status;
+}

@@ -1,0 +1,291 @@
+// potential.cpp - reader of AtomNN's potential text format and builder of the device tables.
+#include "potential.h"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+
+#include "../../include/nnpgpu.h"
+
+namespace nnpgpu {
+
+namespace {
+
+const double kPi = 3.141592653589793;  // math::constant::PI (src/math/const.hpp:9)
+
+std::vector<std::string> split_ws(const std::string& s) {  // string::WS tokens (src/str/string.hpp:16)
+  std::vector<std::string> t;
+  std::string cur;
+  for (char ch : s) {
+    if (ch == ' ' || ch == '\t' || ch == '\r' || ch == '\n') {
+      if (!cur.empty()) t.push_back(cur), cur.clear();
+    } else {
+      cur.push_back(ch);
+    }
+  }
+  if (!cur.empty()) t.push_back(cur);
+  return t;
+}
+
+struct Lines {
+  FILE* f;
+  int lineno = 0;
+  std::vector<std::string> next() {
+    std::string s;
+    int ch;
+    bool any = false;
+    while ((ch = std::fgetc(f)) != EOF) {
+      any = true;
+      if (ch == '\n') break;
+      s.push_back((char)ch);
+    }
+    if (!any) throw PotError(NNPGPU_ERR_IO, "potential file: unexpected end of file after line " + std::to_string(lineno));
+    ++lineno;
+    return split_ws(s);
+  }
+};
+
+const std::string& tok(const std::vector<std::string>& t, size_t i, const Lines& L) {
+  if (i >= t.size()) throw PotError(NNPGPU_ERR_IO, "potential file: missing field on line " + std::to_string(L.lineno));
+  return t[i];
+}
+
+int cut_of(const std::string& s) { return s == "STEP" ? CUT_STEP : s == "COS" ? CUT_COS : s == "TANH" ? CUT_TANH : 0; }
+int norm_of(const std::string& s) { return s == "UNIT" ? 1 : s == "VOL" ? 2 : 0; }
+double norm_value(int norm, double rc) {  // Basis::norm (src/nnp/basis.cpp:160-168)
+  if (norm == 1) return 1.0;
+  return 1.0 / (0.5 * 4.0 / 3.0 * (kPi * kPi - 6.0) / kPi * rc * rc * rc);
+}
+
+}  // namespace
+
+HPot read_potential(const char* path) {
+  FILE* f = std::fopen(path, "r");
+  if (!f) throw PotError(NNPGPU_ERR_IO, std::string("could not open potential file \"") + path + "\"");
+  HPot P;
+  Lines L{f};
+  try {
+    L.next();  // "ann"
+    auto t = L.next();
+    P.ntypes = std::atoi(tok(t, 1, L).c_str());
+    if (P.ntypes <= 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid number of types");
+    P.types.resize(P.ntypes);
+    for (int n = 0; n < P.ntypes; ++n) {  // Type::read (src/nnp/type.cpp:32-70)
+      auto tt = L.next();
+      for (size_t k = 0; k < tt.size(); ++k) {
+        std::string tag = tt[k];
+        if (!tag.empty() && tag[0] == '#') break;
+        for (auto& c : tag) c = (char)std::toupper((unsigned char)c);
+        const bool has = k + 1 < tt.size();
+        if (tag == "NAME" && has) P.types[n].name = tt[++k];
+        else if (tag == "MASS" && has) P.types[n].mass = std::atof(tt[++k].c_str());
+        else if (tag == "ENERGY" && has) P.types[n].energy = std::atof(tt[++k].c_str());
+        else if (has && (tag == "CHARGE" || tag == "CHI" || tag == "ETA" || tag == "JS" || tag == "C6" || tag == "RVDW" ||
+                         tag == "RCOV"))
+          ++k;
+      }
+      P.index[P.types[n].name] = n;
+    }
+    t = L.next();
+    P.rc = std::atof(tok(t, 1, L).c_str());
+    if (!(P.rc > 0)) throw PotError(NNPGPU_ERR_IO, "potential file: invalid cutoff");
+    const int nb = P.ntypes * (P.ntypes + 1) / 2;
+    P.rad.assign(P.ntypes, std::vector<HBasisR>(P.ntypes));
+    P.ang.assign(P.ntypes, std::vector<HBasisA>(nb));
+    auto idx = [&](const std::string& s) {
+      auto it = P.index.find(s);
+      if (it == P.index.end()) throw PotError(NNPGPU_ERR_IO, "potential file: unknown type \"" + s + "\"");
+      return it->second;
+    };
+    for (int i = 0; i < P.ntypes; ++i) {
+      const int II = idx(tok(L.next(), 1, L));
+      for (int j = 0; j < P.ntypes; ++j) {  // BasisR::read (src/nnp/basis_radial.cpp:123-144)
+        const int JJ = idx(tok(L.next(), 1, L));
+        auto h = L.next();
+        HBasisR& b = P.rad[II][JJ];
+        b.norm = norm_of(tok(h, 1, L));
+        b.cut = cut_of(tok(h, 2, L));
+        b.rc = std::atof(tok(h, 3, L).c_str());
+        const std::string phi = tok(h, 4, L);
+        b.phi = phi == "GAUSSIAN" ? 1 : (phi == "TANH" || phi == "SOFTPLUS" || phi == "LOGCOSH" || phi == "SWISH" || phi == "MISH") ? 2 : 0;
+        if (b.phi == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid radial function type " + phi);
+        const int n = std::atoi(tok(h, 5, L).c_str());
+        if (b.norm == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid normalization scheme");
+        if (!(b.rc > 0)) throw PotError(NNPGPU_ERR_IO, "potential file: invalid basis cutoff");
+        for (int k = 0; k < n; ++k) {
+          auto p = L.next();
+          b.rs.push_back(std::atof(tok(p, 0, L).c_str()));
+          b.eta.push_back(std::atof(tok(p, 1, L).c_str()));
+        }
+      }
+      for (int j = 0; j < P.ntypes; ++j)
+        for (int k = j; k < P.ntypes; ++k) {  // BasisA::read (src/nnp/basis_angular.cpp:113-138)
+          auto tt = L.next();
+          const int JJ = idx(tok(tt, 1, L)), KK = idx(tok(tt, 2, L));
+          auto h = L.next();
+          HBasisA& b = P.ang[II][lidx(JJ, KK)];
+          b.norm = norm_of(tok(h, 1, L));
+          b.cut = cut_of(tok(h, 2, L));
+          b.rc = std::atof(tok(h, 3, L).c_str());
+          const std::string phi = tok(h, 4, L);
+          b.phi = phi == "GAUSS" ? 1 : (phi == "IPOWP" || phi == "IPOWS" || phi == "SECHP" || phi == "SECHS") ? 2 : 0;
+          if (b.phi == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid angular function type " + phi);
+          const int n = std::atoi(tok(h, 5, L).c_str());
+          b.alpha = std::atoi(tok(h, 6, L).c_str());
+          if (b.norm == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid normalization scheme");
+          if (!(b.rc > 0)) throw PotError(NNPGPU_ERR_IO, "potential file: invalid basis cutoff");
+          for (int q = 0; q < n; ++q) {
+            auto p = L.next();
+            b.eta.push_back(std::atof(tok(p, 0, L).c_str()));
+            b.zeta.push_back(std::atof(tok(p, 1, L).c_str()));
+            b.lam.push_back(std::atoi(tok(p, 2, L).c_str()));
+          }
+        }
+    }
+    // input layout (NNH::init_input, src/nnp/nnh.cpp:95-121)
+    P.nin.assign(P.ntypes, 0);
+    P.ninR.assign(P.ntypes, 0);
+    P.offR.assign(P.ntypes, std::vector<int>(P.ntypes, 0));
+    P.offA.assign(P.ntypes, std::vector<int>(nb, 0));
+    for (int I = 0; I < P.ntypes; ++I) {
+      int r = 0;
+      for (int J = 0; J < P.ntypes; ++J) { P.offR[I][J] = r; r += (int)P.rad[I][J].rs.size(); }
+      int a = 0;
+      for (int b = 0; b < nb; ++b) { P.offA[I][b] = a; a += (int)P.ang[I][b].eta.size(); }
+      P.ninR[I] = r;
+      P.nin[I] = r + a;
+    }
+    // networks (ANN::read, src/ml/nn.cpp:1349-1425)
+    P.nets.resize(P.ntypes);
+    for (int n = 0; n < P.ntypes; ++n) {
+      const int II = idx(tok(L.next(), 1, L));
+      HNet& net = P.nets[II];
+      auto cfg = L.next();
+      std::vector<int> nodes;
+      for (size_t k = 1; k < cfg.size(); ++k) nodes.push_back(std::atoi(cfg[k].c_str()));
+      if (nodes.size() < 2) throw PotError(NNPGPU_ERR_IO, "potential file: invalid network configuration");
+      net.nin = nodes[0];
+      net.nodes.assign(nodes.begin() + 1, nodes.end());
+      for (int x : nodes)
+        if (x <= 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid layer size");
+      const std::string neuron = tok(L.next(), 1, L);
+      net.act = neuron == "TANH" ? ACT_TANH : neuron == "LINEAR" ? ACT_LINEAR : neuron == "SIGMOID" ? ACT_SIGMOID : -1;
+      if (net.act < 0) {
+        static const char* known[] = {"ISRU", "ARCTAN", "SOFTSIGN", "RELU", "SOFTPLUS", "ELU", "GELU", "SWISH", "MISH",
+                                      "TANHRE", "LOGCOSH", "IQUAD", "IFABS", "SINSIG"};
+        bool k = false;
+        for (const char* s : known) k = k || neuron == s;
+        if (!k) throw PotError(NNPGPU_ERR_IO, "potential file: invalid neuron " + neuron);
+        net.act = 0;  // valid in the reference, not implemented here
+      }
+      const int nout = net.nodes.back();
+      auto vec = [&](std::vector<double>& v, int cnt) {
+        auto p = L.next();
+        v.resize(cnt);
+        for (int k = 0; k < cnt; ++k) v[k] = std::atof(tok(p, k + 1, L).c_str());
+      };
+      vec(net.inpw, net.nin);
+      vec(net.outw, nout);
+      vec(net.inpb, net.nin);
+      vec(net.outb, nout);
+      const int Ln = (int)net.nodes.size();
+      net.b.resize(Ln);
+      net.w.resize(Ln);
+      for (int l = 0; l < Ln; ++l) vec(net.b[l], net.nodes[l]);
+      for (int l = 0; l < Ln; ++l) vec(net.w[l], net.nodes[l] * (l == 0 ? net.nin : net.nodes[l - 1]));
+      if (net.nin != P.nin[II]) throw PotError(NNPGPU_ERR_IO, "potential file: network input size does not match the basis");
+    }
+  } catch (...) {
+    std::fclose(f);
+    throw;
+  }
+  std::fclose(f);
+  return P;
+}
+
+void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
+  auto unsup = [](const std::string& m) { throw PotError(NNPGPU_ERR_UNSUPPORTED, m); };
+  P = PotParams();
+  if (pot.ntypes > NT_MAX) unsup("more than " + std::to_string(NT_MAX) + " atom types");
+  P.ntypes = pot.ntypes;
+  P.rc = (float)pot.rc;
+  ne_max = 1;
+  nz_max = 1;
+  for (int I = 0; I < pot.ntypes; ++I) {
+    if (pot.nin[I] > NIN_MAX) unsup("more than " + std::to_string(NIN_MAX) + " network inputs");
+    P.nin[I] = pot.nin[I];
+    for (int J = 0; J < pot.ntypes; ++J) {
+      const HBasisR& b = pot.rad[I][J];
+      RadialP& r = P.rad[I][J];
+      if (b.phi != 1 && !b.rs.empty()) unsup("radial functions other than GAUSSIAN");
+      if ((int)b.rs.size() > NR_MAX) unsup("more than " + std::to_string(NR_MAX) + " radial functions per pair");
+      if (b.cut == 0) unsup("unknown cutoff function");
+      r.n = (int)b.rs.size();
+      r.off = pot.offR[I][J];
+      r.cut = b.cut;
+      r.rc = (float)b.rc;
+      r.pirc = (float)(kPi / b.rc);
+      r.rci = (float)(1.0 / b.rc);
+      r.norm = (float)norm_value(b.norm, b.rc);
+      for (int k = 0; k < r.n; ++k) { r.rs[k] = (float)b.rs[k]; r.eta[k] = (float)b.eta[k]; }
+    }
+    for (int q = 0; q < pot.ntypes * (pot.ntypes + 1) / 2; ++q) {
+      const HBasisA& b = pot.ang[I][q];
+      AngP& a = P.ang[I][q];
+      const int n = (int)b.eta.size();
+      if (n == 0) continue;
+      if (b.phi != 1) unsup("angular functions other than GAUSS");
+      if (n > NA_MAX) unsup("more than " + std::to_string(NA_MAX) + " angular functions per block");
+      if (b.cut == 0) unsup("unknown cutoff function");
+      if (b.alpha < 1 || b.alpha > 8) unsup("angular power alpha outside 1..8");
+      a.n = n;
+      a.off = pot.ninR[I] + pot.offA[I][q];
+      a.cut = b.cut;
+      a.alpha = b.alpha;
+      a.rc = (float)b.rc;
+      a.pirc = (float)(kPi / b.rc);
+      a.rci = (float)(1.0 / b.rc);
+      a.norm = (float)norm_value(b.norm, b.rc);
+      std::vector<double> ie;   // distinct 1/eta^alpha (BasisA::init, basis_angular.cpp:168-173)
+      std::vector<int> lams;
+      for (int f = 0; f < n; ++f) {
+        double v = 1.0;
+        for (int k = 0; k < b.alpha; ++k) v *= 1.0 / b.eta[f];
+        if (std::find(ie.begin(), ie.end(), v) == ie.end()) ie.push_back(v);
+        if (std::find(lams.begin(), lams.end(), b.lam[f]) == lams.end()) lams.push_back(b.lam[f]);
+      }
+      if ((int)ie.size() > NE_MAX) unsup("more than " + std::to_string(NE_MAX) + " distinct angular widths per block");
+      if ((int)lams.size() > NL) unsup("more than two distinct lambda values per block");
+      a.ne = (int)ie.size();
+      a.nl = (int)lams.size();
+      for (int e = 0; e < a.ne; ++e) a.ietap[e] = (float)ie[e];
+      for (int l = 0; l < NL; ++l) a.lam[l] = l < a.nl ? (float)lams[l] : 0.f;
+      int nz = 1;
+      for (int f = 0; f < n; ++f) {
+        int m = -1;
+        for (int k = 0; k < NZ_MAX; ++k)
+          if (b.zeta[f] == (double)(1 << k)) m = k;
+        if (m < 0) unsup("zeta values other than powers of two up to " + std::to_string(1 << (NZ_MAX - 1)));
+        nz = std::max(nz, m + 1);
+        double v = 1.0;
+        for (int k = 0; k < b.alpha; ++k) v *= 1.0 / b.eta[f];
+        const int e = (int)(std::find(ie.begin(), ie.end(), v) - ie.begin());
+        const int l = (int)(std::find(lams.begin(), lams.end(), b.lam[f]) - lams.begin());
+        a.gidx[f] = (signed char)((e * NL + l) * NZ_MAX + m);
+      }
+      a.nz = nz;
+      ne_max = std::max(ne_max, a.ne);
+      nz_max = std::max(nz_max, nz);
+    }
+    const HNet& net = pot.nets[I];
+    if (net.act <= 0) unsup("network activation not implemented on the GPU");
+    if ((int)net.nodes.size() < 2 || (int)net.nodes.size() > NLAYER_MAX) unsup("networks need 1 to 3 hidden layers");
+    if (net.nodes.back() != 1) unsup("networks with more than one output");
+    for (int x : net.nodes)
+      if (x > HID_MAX) unsup("layers wider than " + std::to_string(HID_MAX));
+  }
+}
+
+}  // namespace nnpgpu

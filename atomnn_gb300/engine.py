@@ -1,0 +1,154 @@
+"""Python binding of the C ABI in include/nnpgpu.h (libnnpgpu.so, built in-tree).
+
+The engine runs only on the GPU: loading fails loudly when the shared library is missing, and
+context creation fails when no CUDA device is present.  There is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libnnpgpu.so")
+
+OK, ERR_INVALID, ERR_IO, ERR_CUDA, ERR_OOM, ERR_CAPACITY, ERR_TIMEOUT, ERR_UNSUPPORTED, ERR_BUSY = 0, -1, -2, -3, -4, -5, -6, -7, -8
+ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
+
+# every symbol the header declares
+EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
+           "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_serve_start", "nnpgpu_submit",
+           "nnpgpu_poll", "nnpgpu_serve_stop"]
+
+_lib = None
+
+
+class NNPGPUError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("nnpgpu error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("max_neighbors", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t),
+                ("verbose", ctypes.c_int)]
+
+
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("max_batch_atoms", ctypes.c_int), ("max_inflight", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t),
+                ("skin", ctypes.c_double), ("flags", ctypes.c_int)]
+
+
+def load_library(path=LIB_PATH):
+    """Load libnnpgpu.so; raises if it has not been built (no fallback exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libnnpgpu.so not built (%s): run `python -c 'import __graft_entry__ as g; g.build()'`" % path)
+    L = ctypes.CDLL(path)
+    vp, ip, dp, cp, szp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_char_p, ctypes.c_size_t
+    L.nnpgpu_create.argtypes = [cp, ctypes.POINTER(Opts), ctypes.POINTER(vp)]
+    L.nnpgpu_destroy.argtypes = [vp]
+    L.nnpgpu_destroy.restype = None
+    L.nnpgpu_last_error.argtypes = [vp]
+    L.nnpgpu_last_error.restype = cp
+    L.nnpgpu_ntypes.argtypes = [vp]
+    L.nnpgpu_type_index.argtypes = [vp, cp]
+    L.nnpgpu_cutoff.argtypes = [vp]
+    L.nnpgpu_cutoff.restype = dp
+    L.nnpgpu_ninput.argtypes = [vp, ip]
+    L.nnpgpu_compute.argtypes = [vp, ip, vp, vp, vp, vp, ip, vp, vp, vp]
+    L.nnpgpu_compute_device.argtypes = [vp, ip, vp, vp, vp, vp, ip, vp, vp, vp, vp]
+    L.nnpgpu_neighbors.argtypes = [vp, ip, vp, vp, ip, vp, vp, vp, vp, vp]
+    L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
+    L.nnpgpu_submit.argtypes = [vp, ip, vp, vp, vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
+    L.nnpgpu_poll.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.POINTER(ctypes.c_double)]
+    L.nnpgpu_serve_stop.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _cell_colmajor(cell):
+    if cell is None:
+        return np.zeros(9)
+    return np.ascontiguousarray(np.asarray(cell, dtype=np.float64).T).ravel()
+
+
+class Engine:
+    """A context of the GPU engine for one potential file (nnpgpu_create)."""
+
+    def __init__(self, potfile, device=0, max_neighbors=0, hbm_budget_bytes=0):
+        self.lib = load_library()
+        self._ctx = ctypes.c_void_p()
+        o = Opts(device, max_neighbors, hbm_budget_bytes, 0)
+        rc = self.lib.nnpgpu_create(potfile.encode(), ctypes.byref(o), ctypes.byref(self._ctx))
+        if rc != OK:
+            msg = self.lib.nnpgpu_last_error(self._ctx).decode() if self._ctx else ""
+            if self._ctx:
+                self.lib.nnpgpu_destroy(self._ctx)
+                self._ctx = None
+            raise NNPGPUError(rc, msg)
+        self.ntypes = self.lib.nnpgpu_ntypes(self._ctx)
+        self.rc = self.lib.nnpgpu_cutoff(self._ctx)
+        self.ninput = [self.lib.nnpgpu_ninput(self._ctx, t) for t in range(self.ntypes)]
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self.lib.nnpgpu_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def _check(self, rc):
+        if rc != OK:
+            raise NNPGPUError(rc, self.lib.nnpgpu_last_error(self._ctx).decode())
+
+    def type_index(self, name):
+        return self.lib.nnpgpu_type_index(self._ctx, name.encode())
+
+    def compute(self, structures, flags=ENERGY | FORCE):
+        """structures: list of objects with .posn (N,3), .species (N,), .cell (3x3, columns =
+        lattice vectors).  Returns (energies [nstruc], forces list [(N,3)] or None, symm or None)."""
+        natoms = np.array([s.posn.shape[0] for s in structures], dtype=np.int32)
+        posn = np.ascontiguousarray(np.concatenate([np.asarray(s.posn, dtype=np.float64) for s in structures]) if len(structures) else np.zeros((0, 3)))
+        species = np.ascontiguousarray(np.concatenate([np.asarray(s.species, dtype=np.int32) for s in structures]) if len(structures) else np.zeros(0, np.int32))
+        cell = np.ascontiguousarray(np.concatenate([_cell_colmajor(s.cell) for s in structures]) if len(structures) else np.zeros(0))
+        n = int(natoms.sum())
+        energy = np.zeros(len(structures)) if flags & ENERGY else None
+        force = np.zeros((n, 3)) if flags & FORCE else None
+        symm = np.zeros((n, max(self.ninput)), dtype=np.float32) if flags & SYMM else None
+        self._check(self.lib.nnpgpu_compute(self._ctx, len(structures), _p(natoms), _p(posn), _p(species), _p(cell), flags, _p(energy),
+                                            _p(force), _p(symm)))
+        forces = None
+        if force is not None:
+            offs = np.concatenate([[0], np.cumsum(natoms)])
+            forces = [force[offs[k]:offs[k + 1]] for k in range(len(structures))]
+        return energy, forces, symm
+
+    def compute_device(self, natoms, d_posn, d_species, cells_colmajor, flags, d_energy=0, d_force=0, d_symm=0, stream=0):
+        """Device-resident variant: d_* are raw device pointers (ints), natoms and cells host arrays."""
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        cells = np.ascontiguousarray(cells_colmajor, dtype=np.float64)
+        self._check(self.lib.nnpgpu_compute_device(self._ctx, len(natoms), _p(natoms), ctypes.c_void_p(d_posn),
+                                                   ctypes.c_void_p(d_species), _p(cells), flags, ctypes.c_void_p(d_energy or None),
+                                                   ctypes.c_void_p(d_force or None), ctypes.c_void_p(d_symm or None),
+                                                   ctypes.c_void_p(stream or None)))
+
+    def neighbors(self, posn, cell, cap=256):
+        """Neighbour list of one structure built on the GPU (reference list order)."""
+        posn = np.ascontiguousarray(posn, dtype=np.float64)
+        n = posn.shape[0]
+        count = np.zeros(n, dtype=np.int32)
+        index = np.zeros((n, cap), dtype=np.int32)
+        r = np.zeros((n, cap, 4), dtype=np.float32)
+        mn = np.zeros((n, cap), dtype=np.uint8)
+        sh = np.zeros((n, cap, 3), dtype=np.int32)
+        self._check(self.lib.nnpgpu_neighbors(self._ctx, n, _p(posn), _p(_cell_colmajor(cell)), cap, _p(count), _p(index), _p(r),
+                                              _p(mn), _p(sh)))
+        return [dict(index=index[i, :count[i]].copy(), r=r[i, :count[i], :3].astype(np.float64), dr=r[i, :count[i], 3].astype(np.float64),
+                     min=mn[i, :count[i]].astype(bool), shift=sh[i, :count[i]].copy()) for i in range(n)]

@@ -1,0 +1,115 @@
+/*
+ * nnpgpu.h - C ABI of the GB300 energy/force engine for Behler-Parrinello potentials.
+ *
+ * Drop-in boundary for the NNP energy/force calls of AtomNN (markdellostritto/AtomNN).
+ * The reference exposes static C++ functions on class NNP (src/nnp/nnp.hpp:108-120) plus
+ * NeighborList::build (src/struc/neighbor.hpp:85); those are not callable through an FFI,
+ * so each entry point below names the reference call(s) it replaces.  Plain pointers and
+ * sizes only; every function returns a status code (0 = ok) instead of throwing, and the
+ * message of the last failure is available from nnpgpu_last_error().
+ *
+ * Units are the potential's (metal: Angstrom, eV).  Cells are 9 doubles, column-major, the
+ * columns being the lattice vectors (Cell::R_, src/struc/cell.hpp); an all-zero cell means a
+ * non-periodic structure.  Positions are Cartesian, natoms*3 doubles.  Species are indices
+ * into the potential's type list (what NNP::index(name) returns, src/nnp/nnp.hpp:83).
+ *
+ * Threading: one context per host thread; a context owns its CUDA stream and device memory.
+ */
+#ifndef NNPGPU_H
+#define NNPGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define NNPGPU_OK 0
+#define NNPGPU_ERR_INVALID (-1)     /* invalid argument or input (NaN position, bad species, singular cell) */
+#define NNPGPU_ERR_IO (-2)          /* potential file could not be read (NNP::read throws, src/nnp/nnp.cpp:190) */
+#define NNPGPU_ERR_CUDA (-3)        /* CUDA runtime error, or no usable GPU */
+#define NNPGPU_ERR_OOM (-4)         /* device allocation failed or the HBM budget would be exceeded */
+#define NNPGPU_ERR_CAPACITY (-5)    /* neighbour capacity exceeded after the automatic retry */
+#define NNPGPU_ERR_TIMEOUT (-6)     /* a bounded wait on the device ran out */
+#define NNPGPU_ERR_UNSUPPORTED (-7) /* potential uses a form the GPU kernels do not implement */
+#define NNPGPU_ERR_BUSY (-8)        /* serving: request not finished yet, or queue full */
+
+/* flags for nnpgpu_compute */
+#define NNPGPU_ENERGY 0x1     /* energy per structure (NNP::energy, src/nnp/nnp.cpp:390-402) */
+#define NNPGPU_FORCE 0x2      /* forces (NNP::force, src/nnp/nnp.cpp:416-482) */
+#define NNPGPU_SYMM 0x4       /* symmetry functions (NNP::symm, src/nnp/nnp.cpp:334-381), FP32 */
+#define NNPGPU_BF16 0x8       /* atomic networks as BF16 tensor-core GEMMs (FP32 accumulate) */
+#define NNPGPU_NO_VACUUM 0x10 /* energy without the species vacuum energy (NNP::compute, src/nnp/nnp.cpp:496-566) */
+#define NNPGPU_BATCHED 0x20   /* all structures in one launch sequence; otherwise one structure at a time */
+
+typedef struct nnpgpu_ctx nnpgpu_ctx;
+
+typedef struct nnpgpu_opts {
+  int device;              /* CUDA device ordinal */
+  int max_neighbors;       /* initial neighbour capacity per atom (0 = automatic); grows on overflow */
+  size_t hbm_budget_bytes; /* cap on the context's device memory (0 = no cap) */
+  int verbose;
+} nnpgpu_opts;
+
+/* Reads a potential file in AtomNN's text format and prepares the device.
+ * Replaces NNP::read(const char*, NNP&) (src/nnp/nnp.cpp:182-191,244-308). */
+int nnpgpu_create(const char* potfile, const nnpgpu_opts* opts, nnpgpu_ctx** out);
+void nnpgpu_destroy(nnpgpu_ctx* ctx);
+const char* nnpgpu_last_error(const nnpgpu_ctx* ctx);
+
+/* Potential queries: NNP::ntypes (nnp.hpp:82), NNP::index(name) (nnp.hpp:83),
+ * NNP::rc (nnp.hpp:90), NNH::nInput (nnh.hpp:91). */
+int nnpgpu_ntypes(const nnpgpu_ctx* ctx);
+int nnpgpu_type_index(const nnpgpu_ctx* ctx, const char* name);
+double nnpgpu_cutoff(const nnpgpu_ctx* ctx);
+int nnpgpu_ninput(const nnpgpu_ctx* ctx, int type);
+
+/* Energy, forces and/or symmetry functions of nstruc structures (host buffers).
+ * Replaces the compute tool's per-structure sequence NeighborList::build + NNP::symm +
+ * NNP::energy + NNP::force (src/nnp/nnpce.cpp:273-281), or NNP::compute with NNPGPU_NO_VACUUM.
+ *   natoms[nstruc], posn[sum(natoms)*3], species[sum(natoms)], cell[nstruc*9]
+ *   energy[nstruc] (FP64) if NNPGPU_ENERGY, force[sum(natoms)*3] (FP64) if NNPGPU_FORCE,
+ *   symm[sum(natoms)*max_ninput] (FP32, row stride = max over types of nnpgpu_ninput) if NNPGPU_SYMM. */
+int nnpgpu_compute(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* posn, const int* species,
+                   const double* cell, int flags, double* energy, double* force, float* symm);
+
+/* Same computation on device-resident data: posn, species, energy, force, symm are device
+ * pointers; natoms and cell stay on the host.  stream is a cudaStream_t (NULL = the context's
+ * stream).  Returns once the work is enqueued; the caller synchronises the stream. */
+int nnpgpu_compute_device(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* d_posn,
+                          const int* d_species, const double* cell, int flags, double* d_energy,
+                          double* d_force, float* d_symm, void* stream);
+
+/* Neighbour list of one structure, built on the GPU.  Replaces NeighborList::build
+ * (src/struc/neighbor.cpp:59-171).  Per atom at most cap entries in the reference's order:
+ * index (neighbour atom), r[4] = (x, y, z, |r|) FP32 with r pointing from the neighbour to the
+ * centre, min flag, shift[3] = integer lattice translation T (r = posn_i - posn_j - R*T).
+ * count[natoms] receives the full sizes; returns NNPGPU_ERR_CAPACITY if some count > cap. */
+int nnpgpu_neighbors(nnpgpu_ctx* ctx, int natoms, const double* posn, const double* cell, int cap,
+                     int* count, int* index, float* r, unsigned char* min, int* shift);
+
+/* ---- serving: continuous batching of energy+force requests (no counterpart in the
+ * reference, whose compute tool evaluates a fixed file list; it serves the same call as
+ * nnpgpu_compute for requests that arrive over time). */
+typedef struct nnpgpu_serve_opts {
+  int max_batch_atoms;     /* atoms admitted into one device batch (0 = automatic) */
+  int max_inflight;        /* batches in flight on the device (>= 1) */
+  size_t hbm_budget_bytes; /* admission budget for resident state + batch buffers (0 = context budget) */
+  double skin;             /* neighbour-list skin for resident structures, Angstrom (0 = rebuild always) */
+  int flags;               /* NNPGPU_BF16 etc. applied to every request */
+} nnpgpu_serve_opts;
+
+int nnpgpu_serve_start(nnpgpu_ctx* ctx, const nnpgpu_serve_opts* opts);
+/* Copies the request; resident_key >= 0 keeps the structure's state on the device between
+ * requests with the same key (MD-style repeat steps), -1 for a one-off request. */
+int nnpgpu_submit(nnpgpu_ctx* ctx, int natoms, const double* posn, const int* species, const double* cell,
+                  long long resident_key, long long* request_id);
+/* NNPGPU_OK when done (results copied out, request released), NNPGPU_ERR_BUSY when not yet. */
+int nnpgpu_poll(nnpgpu_ctx* ctx, long long request_id, double* energy, double* force, double* latency_s);
+int nnpgpu_serve_stop(nnpgpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
