@@ -136,13 +136,13 @@ __device__ __forceinline__ void cell_diff(const StrucMeta& S, double p0, double 
 
 #endif  // __CUDACC__
 
-// Neighbour slot code: bits 0-23 hold the lattice translation (3 x signed 8 bit), bit 24 the
-// minimum-image flag.
+// Neighbour slot code: bits 0-29 hold the lattice translation (3 x 10 bit, offset 512), bit 30
+// the minimum-image flag.
 __host__ __device__ inline int pack_code(int t0, int t1, int t2, bool mn) {
-  return ((t0 + 128) & 0xff) | (((t1 + 128) & 0xff) << 8) | (((t2 + 128) & 0xff) << 16) | (mn ? (1 << 24) : 0);
+  return ((t0 + 512) & 0x3ff) | (((t1 + 512) & 0x3ff) << 10) | (((t2 + 512) & 0x3ff) << 20) | (mn ? (1 << 30) : 0);
 }
-__host__ __device__ inline bool code_min(int c) { return (c >> 24) & 1; }
-__host__ __device__ inline int code_t(int c, int k) { return ((c >> (8 * k)) & 0xff) - 128; }
+__host__ __device__ inline bool code_min(int c) { return (c >> 30) & 1; }
+__host__ __device__ inline int code_t(int c, int k) { return ((c >> (10 * k)) & 0x3ff) - 512; }
 
 #ifdef __CUDACC__
 // ---- cutoff functions (Basis::cut_func / cut_grad, src/nnp/basis.cpp:80-120), FP32

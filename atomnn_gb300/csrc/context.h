@@ -50,7 +50,7 @@ struct nnpgpu_ctx {
   int cap_hint = 0;
   nnpgpu::TuneCfg tune;
   // batch buffers
-  nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, nb_j, nb_r, nb_code, nb_cnt, nb_rev, orphans, G, dEdG, eatom, perm,
+  nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, sfloor, nb_j, nb_r, nb_code, nb_cnt, nb_rev, orphans, G, dEdG, eatom, perm,
       type_count, W, force, energy, status;
   nnpgpu::HostBuf h_meta, h_in, h_out;  // pinned staging: geometry, inputs, outputs
   int buf_generation = 0;
@@ -59,6 +59,11 @@ struct nnpgpu_ctx {
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, int> shapes_seen;
   std::unique_ptr<nnpgpu::Serving> serving;
+  // stage tracing (nnpgpu_profile_*): events at stage boundaries of the batched launch sequence
+  bool prof_on = false;
+  cudaEvent_t prof_ev[NNPGPU_NSTAGES + 1] = {};
+  double prof_ms[NNPGPU_NSTAGES] = {};
+  long long prof_n[NNPGPU_NSTAGES] = {};
 };
 
 namespace nnpgpu {

@@ -21,7 +21,8 @@ struct BatchDev {
   const StrucMeta* meta = nullptr;
   const ImgEntry* imgs = nullptr;
   // neighbour lists
-  float4* sfrac = nullptr;
+  float4* sfrac = nullptr;  // wrapped fractional coordinates
+  int4* sfloor = nullptr;   // their integer floors
   int* nb_j = nullptr;
   float4* nb_r = nullptr;
   int* nb_code = nullptr;

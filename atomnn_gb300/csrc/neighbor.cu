@@ -2,37 +2,53 @@
 //
 // One warp per centre atom.  Lists are written in the reference's order (neighbour atom j
 // ascending, then the reference's lattice-shift enumeration order) into fixed-stride slots
-// [i*cap, i*cap+count_i).  Set membership is decided in FP64 with the reference's own formula
-// (Cell::diff then |diff - R_n|^2 <= rc^2, evaluated in the same order and without FMA
-// contraction), so the pair sets equal the oracle's bit for bit.  An FP32 prefilter on wrapped
-// fractional coordinates discards far pairs before the FP64 test.
+// [i*cap, i*cap+count_i).
+//
+// Decisions are made in FP32 from wrapped fractional coordinates (s = frac(R^-1 r)) and
+// per-atom integer floors, so that the translation Cell::diff picks is known exactly.  Every
+// FP32 decision carries a rounding margin; a pair whose FP32 value falls within the margin of
+// a decision boundary (cutoff, half-cell rounding of Cell::diff, its 6-shift fallback test,
+// equidistant images) is redone in FP64 with the reference's own formula, evaluated in the
+// same order without FMA contraction.  The pair sets therefore equal the oracle's bit for bit
+// while almost no FP64 work is done (GB300's FP64 rate is about 1/64 of its FP32 rate).
 #include "common.cuh"
 #include "kernels.h"
 
 namespace nnpgpu {
 
-// Fractional coordinates wrapped to [0,1), FP32, for the prefilter.
+// Wrapped fractional coordinates (FP32) and integer floors of R^-1 r, per atom.
 __global__ void frac_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, const double* __restrict__ posn,
-                            const int* __restrict__ atom_struc,
-                            const StrucMeta* __restrict__ meta, float4* __restrict__ sfrac, int* __restrict__ status) {
+                            const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta, float4* __restrict__ sfrac,
+                            int4* __restrict__ sfloor, int* __restrict__ status) {
   const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a0 + natoms) return;
   const StrucMeta& S = meta[atom_struc[i]];
   const double p0 = posn[3 * i], p1 = posn[3 * i + 1], p2 = posn[3 * i + 2];
-  if (!isfinite(p0) || !isfinite(p1) || !isfinite(p2)) atomicOr(&status[ST_ERROR], ERR_BAD_POSITION);
+  const bool finite = isfinite(p0) && isfinite(p1) && isfinite(p2);
+  if (!finite) atomicOr(&status[ST_ERROR], ERR_BAD_POSITION);
   if (type && (type[i] < 0 || type[i] >= ntypes)) atomicOr(&status[ST_ERROR], ERR_BAD_TYPE);
   float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (S.mode != 0) {
-    double f0, f1, f2;
-    matvec(S.RInv, p0, p1, p2, f0, f1, f2);
-    f0 -= floor(f0);
-    f1 -= floor(f1);
-    f2 -= floor(f2);
-    s = make_float4((float)f0, (float)f1, (float)f2, 0.f);
+  int4 fl = make_int4(0, 0, 0, 0);
+  if (S.mode != 0 && finite) {
+    double f[3];
+    matvec(S.RInv, p0, p1, p2, f[0], f[1], f[2]);
+    float sf[3];
+    int fi[3];
+    for (int k = 0; k < 3; ++k) {
+      const double fk = floor(f[k]);
+      float v = (float)(f[k] - fk);
+      int q = (fabs(fk) < 1e9) ? (int)fk : 0;
+      if (v >= 1.0f) { v = 0.0f; ++q; }
+      sf[k] = v;
+      fi[k] = q;
+    }
+    s = make_float4(sf[0], sf[1], sf[2], 0.f);
+    fl = make_int4(fi[0], fi[1], fi[2], 0);
   } else {
     s = make_float4((float)p0, (float)p1, (float)p2, 0.f);
   }
   sfrac[i] = s;
+  sfloor[i] = fl;
 }
 
 __device__ __forceinline__ void emit(int slot, int cap, int j, float rx, float ry, float rz, float dr, int code,
@@ -44,17 +60,64 @@ __device__ __forceinline__ void emit(int slot, int cap, int j, float rx, float r
   }
 }
 
+__device__ __forceinline__ void rf_mul(const StrucMeta& S, float d0, float d1, float d2, float& r0, float& r1, float& r2) {
+  r0 = S.Rf[0] * d0 + S.Rf[3] * d1 + S.Rf[6] * d2;
+  r1 = S.Rf[1] * d0 + S.Rf[4] * d1 + S.Rf[7] * d2;
+  r2 = S.Rf[2] * d0 + S.Rf[5] * d1 + S.Rf[8] * d2;
+}
+
+// FP32 version of Cell::diff for the image-shell path.  Returns false when a decision is too
+// close to call in FP32 (the caller then uses the FP64 replay).
+__device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& si, const int4& fi, const float4& sj,
+                                              const int4& fj, float& o0, float& o1, float& o2, int D[3]) {
+  const float eps = 1e-5f;
+  const float dl[3] = {si.x - sj.x, si.y - sj.y, si.z - sj.z};
+  const int di[3] = {fi.x - fj.x, fi.y - fj.y, fi.z - fj.z};
+  float d[3];
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // mod(f,-0.5,0.5) rounds half-integers up: D = floor(f + 0.5)
+    const float t = dl[k] + 0.5f;
+    const float fk = floorf(t);
+    const float fr = t - fk;
+    if (fr < eps || fr > 1.0f - eps) ok = false;
+    d[k] = dl[k] - fk;
+    D[k] = (int)fk + di[k];
+  }
+  rf_mul(S, d[0], d[1], d[2], o0, o1, o2);
+  const float m = S.margin;
+  const float n2 = o0 * o0 + o1 * o1 + o2 * o2;
+  const float dmax2 = (float)S.dMax2;
+  if (fabsf(n2 - dmax2) <= m) ok = false;
+  if (n2 > dmax2) {
+    float best = n2, second = 3.4e38f, b0 = o0, b1 = o1, b2 = o2;
+    int bk = -1;
+    for (int k = 0; k < 6; ++k) {
+      const float t0 = o0 + (float)S.shifts[3 * k], t1 = o1 + (float)S.shifts[3 * k + 1], t2 = o2 + (float)S.shifts[3 * k + 2];
+      const float q = t0 * t0 + t1 * t1 + t2 * t2;
+      if (q < best) { second = best; best = q; b0 = t0; b1 = t1; b2 = t2; bk = k; }
+      else if (q < second) second = q;
+    }
+    if (second - best <= m) ok = false;
+    if (bk >= 0) D[bk / 2] += (bk % 2 == 0) ? -1 : 1;
+    o0 = b0; o1 = b1; o2 = b2;
+  }
+  return ok;
+}
+
 __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int cap, double rc, const double* __restrict__ posn,
-                                                       const float4* __restrict__ sfrac, const int* __restrict__ atom_struc,
-                                                       const StrucMeta* __restrict__ meta, const ImgEntry* __restrict__ imgs,
-                                                       int* __restrict__ nb_j, float4* __restrict__ nb_r,
-                                                       int* __restrict__ nb_code, int* __restrict__ nb_cnt,
-                                                       int* __restrict__ status) {
+                                                       const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
+                                                       const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
+                                                       const ImgEntry* __restrict__ imgs, int* __restrict__ nb_j,
+                                                       float4* __restrict__ nb_r, int* __restrict__ nb_code,
+                                                       int* __restrict__ nb_cnt, int* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
   const StrucMeta& S = meta[atom_struc[i]];
   const double rc2 = rc * rc;
+  const float rc2f = (float)rc2, m = S.margin;
   const int j0 = S.atom0, nj = S.natoms;
   const double pi0 = posn[3 * i], pi1 = posn[3 * i + 1], pi2 = posn[3 * i + 2];
   int* const oj = nb_j + (size_t)i * cap;
@@ -66,57 +129,92 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
   if (S.mode == 2) {
     // single image: keep the Cell::diff image if |diff|^2 <= rc^2 (the only shift is zero)
     const float4 si = sfrac[i];
-    const float rc2hi = (float)rc2 + S.margin;
+    const int4 fi = sfloor[i];
     for (int c = 0; c < nj; c += 32) {
       const int jl = c + lane;
+      const int j = j0 + jl;
       bool keep = false;
-      double o0 = 0, o1 = 0, o2 = 0, d2 = 0;
+      float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       int D[3] = {0, 0, 0};
-      if (jl < nj && j0 + jl != i) {
-        const float4 sj = sfrac[j0 + jl];
-        float d0 = si.x - sj.x, d1 = si.y - sj.y, d2f = si.z - sj.z;
-        d0 -= rintf(d0);
-        d1 -= rintf(d1);
-        d2f -= rintf(d2f);
-        const float r0 = S.Rf[0] * d0 + S.Rf[3] * d1 + S.Rf[6] * d2f;
-        const float r1 = S.Rf[1] * d0 + S.Rf[4] * d1 + S.Rf[7] * d2f;
-        const float r2 = S.Rf[2] * d0 + S.Rf[5] * d1 + S.Rf[8] * d2f;
-        if (r0 * r0 + r1 * r1 + r2 * r2 <= rc2hi) {
-          const int j = j0 + jl;
-          cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], o0, o1, o2, D);
-          d2 = sqn3(o0, o1, o2);
-          keep = d2 <= rc2;
+      if (jl < nj && j != i) {
+        const float4 sj = sfrac[j];
+        const float dl0 = si.x - sj.x, dl1 = si.y - sj.y, dl2 = si.z - sj.z;
+        const float k0 = rintf(dl0), k1 = rintf(dl1), k2 = rintf(dl2);
+        rf_mul(S, dl0 - k0, dl1 - k1, dl2 - k2, r0, r1, r2);
+        const float d2f = r0 * r0 + r1 * r1 + r2 * r2;
+        if (d2f <= rc2f + m) {
+          const int4 fj = sfloor[j];
+          D[0] = (int)k0 + fi.x - fj.x;
+          D[1] = (int)k1 + fi.y - fj.y;
+          D[2] = (int)k2 + fi.z - fj.z;
+          if (d2f < rc2f - m) {
+            keep = true;
+            dr = sqrtf(d2f);
+          } else {
+            double o0, o1, o2;
+            cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], o0, o1, o2, D);
+            const double d2 = sqn3(o0, o1, o2);
+            keep = d2 <= rc2;
+            r0 = (float)o0; r1 = (float)o1; r2 = (float)o2;
+            dr = (float)sqrt(d2);
+          }
         }
       }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (keep) {
-        const int slot = count + __popc(m & lt);
-        emit(slot, cap, j0 + jl, (float)o0, (float)o1, (float)o2, (float)sqrt(d2), pack_code(D[0], D[1], D[2], true), oj, orr, oc);
-      }
-      count += __popc(m);
+      const unsigned mk = __ballot_sync(0xffffffffu, keep);
+      if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc);
+      count += __popc(mk);
     }
   } else if (S.mode == 1) {
     // image shells: for each j, every shift of the box around the Cell::diff image (reference order)
     const ImgEntry* im = imgs + S.img0;
     const int nimg = S.nimg;
+    const float4 si = sfrac[i];
+    const int4 fi = sfloor[i];
     for (int c = 0; c < nj; c += 32) {
       const int jl = c + lane;
       const int j = j0 + jl;
-      double o0 = 0, o1 = 0, o2 = 0;
+      float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+      double p0 = 0, p1 = 0, p2 = 0;
       int D[3] = {0, 0, 0};
       int cnt = 0, best = -1;
+      bool exact = false;  // FP64 replay for this pair
       if (jl < nj) {
-        cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], o0, o1, o2, D);
-        double mn = S.fro;
-        for (int n = 0; n < nimg; ++n) {
-          const double t0 = dsub(o0, im[n].v[0]), t1 = dsub(o1, im[n].v[1]), t2 = dsub(o2, im[n].v[2]);
-          const double d2 = sqn3(t0, t1, t2);
-          const bool keep = (j != i) ? (d2 <= rc2) : (1e-6 < d2 && d2 <= rc2);
-          if (keep) {
-            ++cnt;
-            if (j != i) {
-              const double dr = sqrt(d2);
-              if (dr < mn) { mn = dr; best = n; }
+        bool ok = cell_diff_f32(S, si, fi, sfrac[j], sfloor[j], o0, o1, o2, D);
+        if (ok) {
+          float mn = 3.4e38f, second = 3.4e38f;
+          for (int n = 0; n < nimg; ++n) {
+            const float t0 = o0 - (float)im[n].v[0], t1 = o1 - (float)im[n].v[1], t2 = o2 - (float)im[n].v[2];
+            const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
+            if (fabsf(d2 - rc2f) <= m) { ok = false; break; }
+            const bool keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
+            if (keep) {
+              ++cnt;
+              if (j != i) {
+                if (d2 < mn) { second = mn; mn = d2; best = n; }
+                else if (d2 < second) second = d2;
+              }
+            }
+          }
+          if (ok && second - mn <= m) ok = false;
+          // the reference seeds the minimum search with |R|_F (neighbor.cpp:132)
+          if (ok && best >= 0 && mn >= (float)(S.fro * S.fro) - m) ok = false;
+        }
+        if (!ok) {
+          exact = true;
+          cnt = 0;
+          best = -1;
+          cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], p0, p1, p2, D);
+          double mnd = S.fro;
+          for (int n = 0; n < nimg; ++n) {
+            const double t0 = dsub(p0, im[n].v[0]), t1 = dsub(p1, im[n].v[1]), t2 = dsub(p2, im[n].v[2]);
+            const double d2 = sqn3(t0, t1, t2);
+            const bool keep = (j != i) ? (d2 <= rc2) : (1e-6 < d2 && d2 <= rc2);
+            if (keep) {
+              ++cnt;
+              if (j != i) {
+                const double dr = sqrt(d2);
+                if (dr < mnd) { mnd = dr; best = n; }
+              }
             }
           }
         }
@@ -131,12 +229,22 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       int slot = count + incl - cnt;
       if (cnt > 0) {
         for (int n = 0; n < nimg; ++n) {
-          const double t0 = dsub(o0, im[n].v[0]), t1 = dsub(o1, im[n].v[1]), t2 = dsub(o2, im[n].v[2]);
-          const double d2 = sqn3(t0, t1, t2);
-          const bool keep = (j != i) ? (d2 <= rc2) : (1e-6 < d2 && d2 <= rc2);
+          float t0, t1, t2, dr;
+          bool keep;
+          if (exact) {
+            const double e0 = dsub(p0, im[n].v[0]), e1 = dsub(p1, im[n].v[1]), e2 = dsub(p2, im[n].v[2]);
+            const double d2 = sqn3(e0, e1, e2);
+            keep = (j != i) ? (d2 <= rc2) : (1e-6 < d2 && d2 <= rc2);
+            t0 = (float)e0; t1 = (float)e1; t2 = (float)e2;
+            dr = keep ? (float)sqrt(d2) : 0.f;
+          } else {
+            t0 = o0 - (float)im[n].v[0]; t1 = o1 - (float)im[n].v[1]; t2 = o2 - (float)im[n].v[2];
+            const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
+            keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
+            dr = sqrtf(d2);
+          }
           if (keep) {
-            emit(slot, cap, j, (float)t0, (float)t1, (float)t2, (float)sqrt(d2),
-                 pack_code(D[0] + im[n].n[0], D[1] + im[n].n[1], D[2] + im[n].n[2], n == best), oj, orr, oc);
+            emit(slot, cap, j, t0, t1, t2, dr, pack_code(D[0] + im[n].n[0], D[1] + im[n].n[1], D[2] + im[n].n[2], n == best), oj, orr, oc);
             ++slot;
           }
         }
@@ -145,24 +253,28 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
     }
   } else {
     // non-periodic: plain differences; the reference leaves min=false here (src/struc/neighbor.cpp:149-169)
+    const float4 si = sfrac[i];
     for (int c = 0; c < nj; c += 32) {
       const int jl = c + lane;
       bool keep = false;
-      double t0 = 0, t1 = 0, t2 = 0, d2 = 0;
+      float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       if (jl < nj) {
         const int j = j0 + jl;
-        t0 = dsub(pi0, posn[3 * j]);
-        t1 = dsub(pi1, posn[3 * j + 1]);
-        t2 = dsub(pi2, posn[3 * j + 2]);
-        d2 = sqn3(t0, t1, t2);
-        keep = 1e-6 < d2 && d2 <= rc2;
+        const float4 sj = sfrac[j];
+        const float a = si.x - sj.x, b = si.y - sj.y, cc = si.z - sj.z;
+        const float d2f = a * a + b * b + cc * cc;
+        const float rcw = (float)rc + 0.5f;  // FP32 prefilter only; the decision is FP64
+        if (d2f <= rcw * rcw) {
+          const double t0 = dsub(pi0, posn[3 * j]), t1 = dsub(pi1, posn[3 * j + 1]), t2 = dsub(pi2, posn[3 * j + 2]);
+          const double d2 = sqn3(t0, t1, t2);
+          keep = 1e-6 < d2 && d2 <= rc2;
+          r0 = (float)t0; r1 = (float)t1; r2 = (float)t2;
+          dr = (float)sqrt(d2);
+        }
       }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (keep) {
-        emit(count + __popc(m & lt), cap, j0 + jl, (float)t0, (float)t1, (float)t2, (float)sqrt(d2), pack_code(0, 0, 0, false), oj,
-             orr, oc);
-      }
-      count += __popc(m);
+      const unsigned mk = __ballot_sync(0xffffffffu, keep);
+      if (keep) emit(count + __popc(mk & lt), cap, j0 + jl, r0, r1, r2, dr, pack_code(0, 0, 0, false), oj, orr, oc);
+      count += __popc(mk);
     }
   }
   if (lane == 0) {
@@ -210,10 +322,11 @@ __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int ca
 
 void launch_neighbors(const BatchDev& B, cudaStream_t st) {
   if (B.natoms == 0) return;
-  frac_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.ntypes, B.type, B.posn, B.atom_struc, B.meta, B.sfrac, B.status);
+  frac_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.ntypes, B.type, B.posn, B.atom_struc, B.meta, B.sfrac,
+                                                      B.sfloor, B.status);
   const int blocks = (B.natoms + 3) / 4;
-  neighbor_kernel<<<blocks, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.atom_struc, B.meta, B.imgs, B.nb_j, B.nb_r,
-                                          B.nb_code, B.nb_cnt, B.status);
+  neighbor_kernel<<<blocks, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
+                                          B.nb_j, B.nb_r, B.nb_code, B.nb_cnt, B.status);
 }
 
 void launch_reverse(const BatchDev& B, cudaStream_t st) {

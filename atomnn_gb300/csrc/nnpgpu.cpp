@@ -156,16 +156,28 @@ static int estimate_cap(const nnpgpu_ctx* c, int nstruc, const int* natoms, cons
     best = std::max(best, nb);
   }
   int cap = (int)std::ceil(best / 32.0) * 32;
-  if (c->cap_hint > 0) cap = std::max(cap, c->cap_hint);
+  if (c->cap_hint > 0) cap = (c->cap_hint + 31) / 32 * 32;  // explicit or learned capacity
   return std::min(cap, 256);
 }
 
 int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
   const bool want_force = flags & NNPGPU_FORCE;
   const bool want_energy = flags & NNPGPU_ENERGY;
+  const bool prof = c->prof_on && (flags & NNPGPU_BATCHED);
+  cudaStreamCaptureStatus cap_state = cudaStreamCaptureStatusNone;
+  if (prof) cudaStreamIsCapturing(st, &cap_state);
+  // inside a capture the events become external event-record nodes of the graph
+  const unsigned ev_flags = (cap_state == cudaStreamCaptureStatusActive) ? cudaEventRecordExternal : cudaEventRecordDefault;
+  auto mark = [&](int k) {
+    if (prof) cudaEventRecordWithFlags(c->prof_ev[k], st, ev_flags);
+  };
+  mark(0);
   launch_neighbors(B, st);
+  mark(1);
   if (want_force) launch_reverse(B, st);
+  mark(2);
   if (launch_symm(B, c->P, c->ne, c->nz, c->tune.warps_symm, st) != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "no symm kernel instance");
+  mark(3);
   if (want_energy || want_force) {
     launch_type_sort(B, c->pot.ntypes, st);
     if (flags & NNPGPU_BF16) {
@@ -174,10 +186,16 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
     } else {
       launch_network_fp32(B, c->nets, c->pot.ntypes, c->tune.nn_tile, st);
     }
+    mark(4);
     if (want_force)
       if (launch_force(B, c->P, c->ne, c->nz, c->tune.warps_force, st) != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "no force kernel instance");
+    mark(5);
     launch_gather(B, c->nets, !(flags & NNPGPU_NO_VACUUM), want_force, st);
+  } else {
+    mark(4);
+    mark(5);
   }
+  mark(6);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   return NNPGPU_OK;
@@ -218,7 +236,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
   bool ok = true;
   ok = ok && ensure(c, c->posn, sizeof(double) * 3 * N) && ensure(c, c->type, sizeof(int) * N) &&
        ensure(c, c->atom_struc, sizeof(int) * N) && ensure(c, c->meta, sizeof(StrucMeta) * std::max(nstruc, 1)) &&
-       ensure(c, c->imgs, sizeof(ImgEntry) * imgs.size()) && ensure(c, c->sfrac, sizeof(float4) * N) &&
+       ensure(c, c->imgs, sizeof(ImgEntry) * imgs.size()) && ensure(c, c->sfrac, sizeof(float4) * N) && ensure(c, c->sfloor, sizeof(int4) * N) &&
        ensure(c, c->nb_j, sizeof(int) * NC) && ensure(c, c->nb_r, sizeof(float4) * NC) && ensure(c, c->nb_code, sizeof(int) * NC) &&
        ensure(c, c->nb_cnt, sizeof(int) * N) && ensure(c, c->nb_rev, sizeof(int) * NC) && ensure(c, c->orphans, sizeof(int) * N) &&
        ensure(c, c->G, sizeof(float) * N * c->gstride) && ensure(c, c->dEdG, sizeof(float) * N * c->gstride) &&
@@ -258,6 +276,7 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.meta = (const StrucMeta*)c->meta.p;
   B.imgs = (const ImgEntry*)c->imgs.p;
   B.sfrac = (float4*)c->sfrac.p;
+  B.sfloor = (int4*)c->sfloor.p;
   B.nb_j = (int*)c->nb_j.p;
   B.nb_r = (float4*)c->nb_r.p;
   B.nb_code = (int*)c->nb_code.p;
@@ -315,6 +334,19 @@ int enqueue(nnpgpu_ctx* c, const Uploaded& U, const BatchDev& Ball, int flags, c
     if (rc != NNPGPU_OK) return rc;
   }
   return NNPGPU_OK;
+}
+
+void accumulate_profile(nnpgpu_ctx* c, int flags) {
+  if (!c->prof_on || !(flags & NNPGPU_BATCHED)) return;
+  for (int k = 0; k < NNPGPU_NSTAGES; ++k) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->prof_ev[k], c->prof_ev[k + 1]) == cudaSuccess) {
+      c->prof_ms[k] += ms;
+      c->prof_n[k] += 1;
+    } else {
+      cudaGetLastError();
+    }
+  }
 }
 
 void drop_graphs(nnpgpu_ctx* c) {
@@ -432,7 +464,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   if (!c) return;
   c->serving.reset();
   drop_graphs(c);
-  DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
+  DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
                     &c->status};
   for (DevBuf* b : bufs)
@@ -442,8 +474,37 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   if (c->h_meta.p) cudaFreeHost(c->h_meta.p);
   if (c->h_in.p) cudaFreeHost(c->h_in.p);
   if (c->h_out.p) cudaFreeHost(c->h_out.p);
+  for (int k = 0; k <= NNPGPU_NSTAGES; ++k)
+    if (c->prof_ev[k]) cudaEventDestroy(c->prof_ev[k]);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+extern "C" int nnpgpu_profile_enable(nnpgpu_ctx* c, int on) {
+  if (!c || !c->stream) return NNPGPU_ERR_INVALID;
+  if (on && !c->prof_ev[0])
+    for (int k = 0; k <= NNPGPU_NSTAGES; ++k)
+      if (cudaEventCreate(&c->prof_ev[k]) != cudaSuccess) return cuda_fail(c, cudaGetLastError(), "cudaEventCreate");
+  // graphs captured with a different tracing setting must not be replayed
+  if ((on != 0) != c->prof_on) {
+    drop_graphs(c);
+    c->shapes_seen.clear();
+  }
+  c->prof_on = on != 0;
+  for (int k = 0; k < NNPGPU_NSTAGES; ++k) { c->prof_ms[k] = 0; c->prof_n[k] = 0; }
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_profile_read(const nnpgpu_ctx* c, int stage, double* total_ms, long long* count) {
+  if (!c || stage < 0 || stage >= NNPGPU_NSTAGES) return NNPGPU_ERR_INVALID;
+  if (total_ms) *total_ms = c->prof_ms[stage];
+  if (count) *count = c->prof_n[stage];
+  return NNPGPU_OK;
+}
+
+extern "C" const char* nnpgpu_profile_stage_name(int stage) {
+  static const char* names[NNPGPU_NSTAGES] = {"neighbors", "transpose", "descriptors", "networks", "chain_rule", "gather_energy"};
+  return (stage >= 0 && stage < NNPGPU_NSTAGES) ? names[stage] : "?";
 }
 
 extern "C" const char* nnpgpu_last_error(const nnpgpu_ctx* c) { return c ? c->err.c_str() : "no context"; }
@@ -519,6 +580,7 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
       if (need > 0) { cap = need; c->cap_hint = std::max(c->cap_hint, need); continue; }
       if (flags & NNPGPU_ENERGY) std::memcpy(energy, h, sizeof(double) * nstruc);
       if (flags & NNPGPU_FORCE) std::memcpy(force, h + sizeof(double) * nstruc, sizeof(double) * 3 * N);
+      accumulate_profile(c, flags);
       return NNPGPU_OK;
     }
     if (flags & NNPGPU_SYMM)
@@ -530,6 +592,7 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
     const int need = check_status(c, hstat, U.cap);
     if (need < 0) return need;
     if (need > 0) { cap = need; c->cap_hint = std::max(c->cap_hint, need); continue; }
+    accumulate_profile(c, flags);
     return NNPGPU_OK;
   }
   return set_error(c, NNPGPU_ERR_CAPACITY, "neighbour capacity retries exhausted");

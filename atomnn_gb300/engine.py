@@ -17,7 +17,8 @@ ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 # every symbol the header declares
 EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_serve_start", "nnpgpu_submit",
-           "nnpgpu_poll", "nnpgpu_serve_stop"]
+           "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
+           "nnpgpu_profile_stage_name"]
 
 _lib = None
 
@@ -64,6 +65,10 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_submit.argtypes = [vp, ip, vp, vp, vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
     L.nnpgpu_poll.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.POINTER(ctypes.c_double)]
     L.nnpgpu_serve_stop.argtypes = [vp]
+    L.nnpgpu_profile_enable.argtypes = [vp, ip]
+    L.nnpgpu_profile_read.argtypes = [vp, ip, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_longlong)]
+    L.nnpgpu_profile_stage_name.argtypes = [ip]
+    L.nnpgpu_profile_stage_name.restype = cp
     _lib = L
     return L
 
@@ -130,6 +135,11 @@ class Engine:
             forces = [force[offs[k]:offs[k + 1]] for k in range(len(structures))]
         return energy, forces, symm
 
+    def compute_flat(self, natoms, posn, species, cells_colmajor, flags, energy=None, force=None, symm=None):
+        """nnpgpu_compute on pre-packed host arrays (outputs written in place)."""
+        self._check(self.lib.nnpgpu_compute(self._ctx, len(natoms), _p(natoms), _p(posn), _p(species), _p(cells_colmajor), flags,
+                                            _p(energy), _p(force), _p(symm)))
+
     def compute_device(self, natoms, d_posn, d_species, cells_colmajor, flags, d_energy=0, d_force=0, d_symm=0, stream=0):
         """Device-resident variant: d_* are raw device pointers (ints), natoms and cells host arrays."""
         natoms = np.ascontiguousarray(natoms, dtype=np.int32)
@@ -138,6 +148,18 @@ class Engine:
                                                    ctypes.c_void_p(d_species), _p(cells), flags, ctypes.c_void_p(d_energy or None),
                                                    ctypes.c_void_p(d_force or None), ctypes.c_void_p(d_symm or None),
                                                    ctypes.c_void_p(stream or None)))
+
+    def profile_enable(self, on=True):
+        self._check(self.lib.nnpgpu_profile_enable(self._ctx, 1 if on else 0))
+
+    def profile_read(self):
+        """{stage name: (total ms, count)} of the batched launch sequence since profile_enable."""
+        out = {}
+        for k in range(6):
+            ms, n = ctypes.c_double(), ctypes.c_longlong()
+            self._check(self.lib.nnpgpu_profile_read(self._ctx, k, ctypes.byref(ms), ctypes.byref(n)))
+            out[self.lib.nnpgpu_profile_stage_name(k).decode()] = (ms.value, n.value)
+        return out
 
     def neighbors(self, posn, cell, cap=256):
         """Neighbour list of one structure built on the GPU (reference list order)."""

@@ -47,7 +47,7 @@ typedef struct nnpgpu_ctx nnpgpu_ctx;
 
 typedef struct nnpgpu_opts {
   int device;              /* CUDA device ordinal */
-  int max_neighbors;       /* initial neighbour capacity per atom (0 = automatic); grows on overflow */
+  int max_neighbors;       /* initial neighbour capacity per atom (0 = estimate from density); grows on overflow */
   size_t hbm_budget_bytes; /* cap on the context's device memory (0 = no cap) */
   int verbose;
 } nnpgpu_opts;
@@ -76,7 +76,8 @@ int nnpgpu_compute(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double*
 
 /* Same computation on device-resident data: posn, species, energy, force, symm are device
  * pointers; natoms and cell stay on the host.  stream is a cudaStream_t (NULL = the context's
- * stream).  Returns once the work is enqueued; the caller synchronises the stream. */
+ * stream).  Returns after the stream has finished the work: the status words are read back so
+ * that a neighbour-capacity overflow is retried inside the call. */
 int nnpgpu_compute_device(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* d_posn,
                           const int* d_species, const double* cell, int flags, double* d_energy,
                           double* d_force, float* d_symm, void* stream);
@@ -88,6 +89,14 @@ int nnpgpu_compute_device(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const 
  * count[natoms] receives the full sizes; returns NNPGPU_ERR_CAPACITY if some count > cap. */
 int nnpgpu_neighbors(nnpgpu_ctx* ctx, int natoms, const double* posn, const double* cell, int cap,
                      int* count, int* index, float* r, unsigned char* min, int* shift);
+
+/* ---- stage tracing (diagnostics; the reference times phases with util/Clock, e.g.
+ * src/nnp/nnpte.cpp:1971-1990).  When enabled, CUDA events bracket each stage of the batched
+ * launch sequence and their durations accumulate per stage.  Enabling resets the counters. */
+#define NNPGPU_NSTAGES 6 /* 0 neighbours, 1 transpose, 2 descriptors, 3 networks, 4 chain rule, 5 gather+energy */
+int nnpgpu_profile_enable(nnpgpu_ctx* ctx, int on);
+int nnpgpu_profile_read(const nnpgpu_ctx* ctx, int stage, double* total_ms, long long* count);
+const char* nnpgpu_profile_stage_name(int stage);
 
 /* ---- serving: continuous batching of energy+force requests (no counterpart in the
  * reference, whose compute tool evaluates a fixed file list; it serves the same call as

@@ -1,0 +1,78 @@
+"""CPU tests of the C ABI library: it builds, loads, exports every declared symbol, and
+fails loudly (status codes + messages) without touching a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import REPO, GOLDEN
+
+
+def _declared():
+    with open(os.path.join(REPO, "include", "nnpgpu.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"\b(nnpgpu_\w+)\s*\(", text)))
+
+
+def test_exports_every_declared_symbol(native_lib):
+    names = _declared()
+    assert len(names) >= 14
+    for n in names:
+        assert hasattr(native_lib, n), n
+    from atomnn_gb300 import engine
+    assert set(engine.EXPORTS) == set(names)
+
+
+def _create(lib, path):
+    from atomnn_gb300 import engine
+    ctx = ctypes.c_void_p()
+    rc = lib.nnpgpu_create(path.encode(), None, ctypes.byref(ctx))
+    msg = lib.nnpgpu_last_error(ctx).decode() if ctx else ""
+    if ctx:
+        lib.nnpgpu_destroy(ctx)
+    return rc, msg
+
+
+def test_missing_potential_is_io_error(native_lib, tmp_path):
+    from atomnn_gb300 import engine
+    rc, msg = _create(native_lib, str(tmp_path / "nope.nnp"))
+    assert rc == engine.ERR_IO and "could not open" in msg
+
+
+def test_truncated_potential_is_io_error(native_lib, tmp_path):
+    from atomnn_gb300 import engine
+    src = open(os.path.join(GOLDEN, "small64.nnp")).read().splitlines()
+    p = tmp_path / "cut.nnp"
+    p.write_text("\n".join(src[:40]) + "\n")
+    rc, msg = _create(native_lib, str(p))
+    assert rc == engine.ERR_IO, msg
+
+
+def test_unsupported_forms_are_reported(native_lib, tmp_path):
+    """A zeta that is not a power of two is valid for the reference but not for the GPU kernels."""
+    from atomnn_gb300 import engine
+    lines = open(os.path.join(GOLDEN, "small64.nnp")).read().splitlines()
+    out, done = [], False
+    for ln in lines:
+        parts = ln.split()
+        if not done and len(parts) == 3 and ln.startswith("\t") and parts[1] == "1.000000":
+            ln = "\t%s 3.000000 %s" % (parts[0], parts[2])
+            done = True
+        out.append(ln)
+    assert done
+    p = tmp_path / "z3.nnp"
+    p.write_text("\n".join(out) + "\n")
+    rc, msg = _create(native_lib, str(p))
+    assert rc == engine.ERR_UNSUPPORTED and "zeta" in msg
+
+
+def test_no_gpu_fails_loudly(native_lib, pot_small64):
+    """Without a CUDA device the engine refuses to run: there is no CPU fallback."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from atomnn_gb300 import engine
+    with pytest.raises(engine.NNPGPUError) as ei:
+        engine.Engine(pot_small64)
+    assert ei.value.code == engine.ERR_CUDA

@@ -1,0 +1,203 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the FP64 oracle and the golden
+fixtures.  Tolerances: neighbour lists exact (pair sets, list order, minimum-image flags,
+lattice translations); FP32 path energy <= 1e-5 eV/atom and forces <= 1e-4 eV/A (max abs);
+symmetry functions <= 1e-5 relative to the largest value of the structure."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, load_golden
+from atomnn_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-5   # eV/atom, FP32 path
+F_TOL = 1e-4   # eV/A max abs, FP32 path
+G_TOL = 1e-5   # relative to max |G|
+
+
+@pytest.fixture(scope="module")
+def engines(native_lib):
+    from atomnn_gb300 import engine
+    e1 = engine.Engine(os.path.join(GOLDEN, "small64.nnp"))
+    e2 = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"))
+    yield {"small64": e1, "mixed512": e2}
+    e1.close()
+    e2.close()
+
+
+@pytest.fixture(scope="module")
+def oracles(oracle_lib):
+    return {k: oracle_lib.OracleNNP(os.path.join(GOLDEN, k + ".nnp")) for k in ("small64", "mixed512")}
+
+
+def _flags(*names):
+    from atomnn_gb300 import engine
+    f = 0
+    for n in names:
+        f |= getattr(engine, n)
+    return f
+
+
+def _assert_lists_equal(g, o):
+    assert len(g) == len(o)
+    for i in range(len(o)):
+        np.testing.assert_array_equal(g[i]["index"], o[i]["index"])
+        np.testing.assert_array_equal(g[i]["shift"], o[i]["shift"])
+        np.testing.assert_array_equal(g[i]["min"], o[i]["min"])
+        if len(o[i]["r"]):
+            np.testing.assert_allclose(g[i]["r"], o[i]["r"], rtol=0, atol=2e-5)
+
+
+def _assert_ef(e, F, eo, Fo, n):
+    assert abs(e - eo) / n <= E_TOL, (e, eo)
+    assert np.abs(F - Fo).max() <= F_TOL
+
+
+@pytest.mark.parametrize("name", ["small64", "mixed3", "cluster20"])
+def test_golden_neighbors(engines, name):
+    pot = str(np.load(os.path.join(GOLDEN, name + ".npz"))["potential"][0])
+    for s, ref in load_golden(name):
+        g = engines[pot].neighbors(s.posn, s.cell)
+        np.testing.assert_array_equal([len(x["index"]) for x in g], ref["nb_count"])
+        np.testing.assert_array_equal(np.concatenate([x["index"] for x in g]), ref["nb_index"])
+        np.testing.assert_array_equal(np.concatenate([x["shift"] for x in g]), ref["nb_shift"])
+        np.testing.assert_array_equal(np.concatenate([x["min"] for x in g]).astype(np.uint8), ref["nb_min"])
+
+
+@pytest.mark.parametrize("name", ["small64", "mixed3", "cluster20"])
+@pytest.mark.parametrize("batched", [False, True])
+def test_golden_energy_force_symm(engines, name, batched):
+    pot = str(np.load(os.path.join(GOLDEN, name + ".npz"))["potential"][0])
+    cases = load_golden(name)
+    strucs = [s for s, _ in cases]
+    flags = _flags("ENERGY", "FORCE", "SYMM") | (_flags("BATCHED") if batched else 0)
+    e, F, G = engines[pot].compute(strucs, flags)
+    off = 0
+    for k, (s, ref) in enumerate(cases):
+        _assert_ef(e[k], F[k], ref["energy"][0], ref["force"], s.natoms)
+        Gs = G[off:off + s.natoms, :ref["symm"].shape[1]]
+        off += s.natoms
+        assert np.abs(Gs - ref["symm"]).max() <= G_TOL * max(np.abs(ref["symm"]).max(), 1.0)
+
+
+def test_compute_semantics_no_vacuum(engines):
+    cases = load_golden("mixed3")
+    e, _, _ = engines["mixed512"].compute([s for s, _ in cases], _flags("ENERGY", "FORCE", "NO_VACUUM", "BATCHED"))
+    for k, (s, ref) in enumerate(cases):
+        assert abs(e[k] - ref["energy_compute"][0]) / s.natoms <= E_TOL
+
+
+def test_batched_equals_plain(engines):
+    strucs = W.make_structures("mixed512", seed=21, count=12)
+    a = engines["mixed512"].compute(strucs, _flags("ENERGY", "FORCE"))
+    b = engines["mixed512"].compute(strucs, _flags("ENERGY", "FORCE", "BATCHED"))
+    np.testing.assert_array_equal(a[0], b[0])
+    for x, y in zip(a[1], b[1]):
+        np.testing.assert_array_equal(x, y)
+
+
+def _sheared_cell(rng):
+    # strongly sheared cell: exercises the 6-shift fallback of Cell::diff and many images
+    cell = W.lattice(7.0, 7.5, 8.0, 60.0, 115.0, 65.0)
+    return W.Structure(posn=rng.uniform(0, 1, size=(24, 3)) @ cell.T, species=(np.arange(24) % 2).astype(np.int32), cell=cell)
+
+
+def _perfect_lattice():
+    # exact lattice sites: equidistant images tie, the first image in list order is the minimum
+    m, a = 3, 2.8
+    idx = np.array([(x, y, z) for x in range(m) for y in range(m) for z in range(m)], dtype=float)
+    return W.Structure(posn=idx * a, species=(np.arange(27) % 3 == 0).astype(np.int32), cell=np.eye(3) * m * a)
+
+
+@pytest.mark.parametrize("case", ["sheared", "perfect", "one_atom", "two_atoms", "isolated", "big_cell"])
+def test_edge_cases_against_oracle(engines, oracles, case):
+    rng = np.random.default_rng(4)
+    if case == "sheared":
+        s = _sheared_cell(rng)
+    elif case == "perfect":
+        s = _perfect_lattice()
+    elif case == "one_atom":
+        s = W.Structure(posn=np.array([[0.3, 0.2, 0.1]]), species=np.array([1], np.int32), cell=np.eye(3) * 4.0)
+    elif case == "two_atoms":
+        s = W.Structure(posn=np.array([[0.0, 0.0, 0.0], [1.9, 0.4, 0.2]]), species=np.array([0, 1], np.int32),
+                        cell=W.lattice(5.0, 5.5, 6.0, 90.0, 95.0, 85.0))
+    elif case == "isolated":
+        p = np.array([[0, 0, 0], [2.0, 0, 0], [0, 2.1, 0], [30.0, 30.0, 30.0]])
+        s = W.Structure(posn=p, species=np.array([0, 1, 1, 0], np.int32), cell=np.zeros((3, 3)))
+    else:
+        s = W.make_structures("cell1728")[0]
+    from oracle import pyoracle
+    o_nb = pyoracle.neighbors(oracles["mixed512"].rc, s.posn, s.cell)
+    _assert_lists_equal(engines["mixed512"].neighbors(s.posn, s.cell), o_nb)
+    eo, Fo, _ = oracles["mixed512"].compute(s.posn, s.species, s.cell, force=True)
+    e, F, _ = engines["mixed512"].compute([s], _flags("ENERGY", "FORCE", "BATCHED"))
+    _assert_ef(e[0], F[0], eo, Fo, s.natoms)
+
+
+def test_empty_structures_in_batch(engines, oracles):
+    strucs = W.make_structures("mixed512", seed=8, count=3, sizes=[20, 30, 25])
+    empty = W.Structure(posn=np.zeros((0, 3)), species=np.zeros(0, np.int32), cell=np.eye(3) * 10)
+    batch = [strucs[0], empty, strucs[1], strucs[2]]
+    e, F, _ = engines["mixed512"].compute(batch, _flags("ENERGY", "FORCE", "BATCHED"))
+    assert e[1] == 0.0 and F[1].shape == (0, 3)
+    for k, s in ((0, strucs[0]), (2, strucs[1]), (3, strucs[2])):
+        eo, Fo, _ = oracles["mixed512"].compute(s.posn, s.species, s.cell, force=True)
+        _assert_ef(e[k], F[k], eo, Fo, s.natoms)
+    e0, _, _ = engines["mixed512"].compute([], _flags("ENERGY", "BATCHED"))
+    assert len(e0) == 0
+
+
+def test_capacity_retry(native_lib, oracles):
+    """A too-small neighbour capacity overflows on the device, is detected and retried."""
+    from atomnn_gb300 import engine
+    eng = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"), max_neighbors=32)
+    s2 = W.make_structures("mixed512", seed=31, count=1, sizes=[300])[0]
+    e, F, _ = eng.compute([s2], _flags("ENERGY", "FORCE", "BATCHED"))
+    eo, Fo, _ = oracles["mixed512"].compute(s2.posn, s2.species, s2.cell, force=True)
+    _assert_ef(e[0], F[0], eo, Fo, s2.natoms)
+    eng.close()
+
+
+def test_invalid_inputs_rejected(engines):
+    from atomnn_gb300 import engine
+    s = W.make_structures("mixed512", seed=8, count=1, sizes=[20])[0]
+    bad = W.Structure(posn=s.posn.copy(), species=s.species, cell=s.cell)
+    bad.posn[3, 1] = np.nan
+    with pytest.raises(engine.NNPGPUError) as ei:
+        engines["mixed512"].compute([bad], _flags("ENERGY", "FORCE", "BATCHED"))
+    assert ei.value.code == engine.ERR_INVALID
+    bad2 = W.Structure(posn=s.posn, species=s.species + 5, cell=s.cell)
+    with pytest.raises(engine.NNPGPUError) as ei:
+        engines["mixed512"].compute([bad2], _flags("ENERGY", "FORCE", "BATCHED"))
+    assert ei.value.code == engine.ERR_INVALID
+    bad3 = W.Structure(posn=s.posn, species=s.species, cell=np.array([[1.0, 2, 3], [2, 4, 6], [0, 0, 1]]))
+    with pytest.raises(engine.NNPGPUError) as ei:
+        engines["mixed512"].compute([bad3], _flags("ENERGY", "FORCE", "BATCHED"))
+    assert ei.value.code == engine.ERR_INVALID
+    # the context stays usable after rejected input
+    e, _, _ = engines["mixed512"].compute([s], _flags("ENERGY", "BATCHED"))
+    assert np.isfinite(e[0])
+
+
+def test_full_size_properties(engines):
+    """At full size (65536-atom cell, 13824-atom supercell) where the oracle is too slow:
+    translation invariance, zero net force in wide cells, and extensivity under replication."""
+    eng = engines["mixed512"]
+    big = W.make_structures("cell65536")[0]
+    e1, F1, _ = eng.compute([big], _flags("ENERGY", "FORCE", "BATCHED"))
+    assert np.abs(F1[0].sum(axis=0)).max() < 1e-6 * big.natoms
+    shifted = W.Structure(posn=big.posn + np.array([1.37, -2.11, 0.53]), species=big.species, cell=big.cell)
+    e2, F2, _ = eng.compute([shifted], _flags("ENERGY", "FORCE", "BATCHED"))
+    assert abs(e1[0] - e2[0]) / big.natoms < E_TOL
+    assert np.abs(F1[0] - F2[0]).max() < F_TOL
+    c = W.make_structures("cell1728")[0]
+    reps = [(i, j, k) for i in range(2) for j in range(2) for k in range(2)]
+    sup = W.Structure(posn=np.concatenate([c.posn + c.cell @ np.array(r, float) for r in reps]),
+                      species=np.concatenate([c.species] * 8), cell=c.cell * 2)
+    ec, Fc, _ = eng.compute([c], _flags("ENERGY", "FORCE", "BATCHED"))
+    es, Fs, _ = eng.compute([sup], _flags("ENERGY", "FORCE", "BATCHED"))
+    assert abs(es[0] / sup.natoms - ec[0] / c.natoms) < E_TOL
+    for r in range(8):
+        assert np.abs(Fs[0][r * 1728:(r + 1) * 1728] - Fc[0]).max() < F_TOL
