@@ -113,8 +113,239 @@ __device__ void block_pair_factors(const WarpSmem& S, const AngP& A, int lo, int
   }
 }
 
-// ------------------------------------------------------------------------------------ symm
+// ------------------------------------------------------------------------------------ blocks
+// Geometry of the circulant schedule of one angular block.
+struct Sched {
+  int xb, nown, yb, mod, d0, d1, nJ;
+  bool tri;
+};
+__device__ __forceinline__ Sched make_sched(int J, int K, int j0, int nJ, int k0, int nK) {
+  Sched s;
+  s.tri = (J == K);
+  s.nJ = nJ;
+  if (s.tri) { s.xb = j0; s.yb = j0; s.nown = nJ; s.mod = nJ; s.d0 = 1; s.d1 = nJ / 2; }
+  else if (nJ <= nK) { s.xb = j0; s.nown = nJ; s.yb = k0; s.mod = nK; s.d0 = 0; s.d1 = nK - 1; }
+  else { s.xb = k0; s.nown = nK; s.yb = j0; s.mod = nJ; s.d0 = 0; s.d1 = nJ - 1; }
+  if (s.nown == 0 || (s.tri && nJ < 2)) s.d1 = s.d0 - 1;
+  return s;
+}
+
+// G4 sums of one block on the (eta) x (lambda) x (zeta = 2^m) grid, NE x NL x NZ, written to
+// scratch[(e*NL+l)*NZ_MAX+m] (BasisA::symm, basis_angular.cpp:406-421; NNP::symm, nnp.cpp:359-377).
 template <int NE, int NZ>
+__device__ __forceinline__ void symm_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  const int lane = threadIdx.x & 31;
+  float acc[NE][NL][NZ];
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) acc[e][l][m] = 0.f;
+  const float lam0 = A.lam[0], lam1 = A.lam[1];
+  const float* __restrict__ ux = S.ux;
+  const float* __restrict__ uy = S.uy;
+  const float* __restrict__ uz = S.uz;
+  const float* __restrict__ ex = S.ex;
+  for (int q = 0; q * 32 < sc.nown; ++q) {
+    const int x = q * 32 + lane;
+    const int a = sc.xb + min(x, sc.nown - 1);
+    const float uax = ux[a], uay = uy[a], uaz = uz[a];
+    float exa[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) exa[e] = ex[e * cap + a];
+    // two rounds per iteration: independent dependency chains for latency hiding
+    for (int dd = sc.d0; dd <= sc.d1; dd += 2) {
+      const int nx1 = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+      const int nx2 = (dd + 1 > sc.d1) ? 0 : ((sc.tri && 2 * (dd + 1) == sc.nJ) ? (sc.nJ >> 1) : sc.nown);
+      const bool v1 = x < nx1, v2 = x < nx2;
+      int y1 = x + dd, y2 = x + dd + 1;
+      if (y1 >= sc.mod) y1 -= sc.mod;
+      if (y2 >= sc.mod) y2 -= sc.mod;
+      const int b1 = sc.yb + (v1 ? y1 : 0), b2 = sc.yb + (v2 ? y2 : 0);
+      const float w1 = v1 ? 1.0f : 0.0f, w2 = v2 ? 1.0f : 0.0f;
+      const float cs1 = uax * ux[b1] + uay * uy[b1] + uaz * uz[b1];
+      const float cs2 = uax * ux[b2] + uay * uy[b2] + uaz * uz[b2];
+      float p1[NL][NZ], p2[NL][NZ];
+      p1[0][0] = fabsf(0.5f * (1.0f + lam0 * cs1));
+      p1[1][0] = fabsf(0.5f * (1.0f + lam1 * cs1));
+      p2[0][0] = fabsf(0.5f * (1.0f + lam0 * cs2));
+      p2[1][0] = fabsf(0.5f * (1.0f + lam1 * cs2));
+#pragma unroll
+      for (int l = 0; l < NL; ++l)
+#pragma unroll
+        for (int m = 1; m < NZ; ++m) {
+          p1[l][m] = p1[l][m - 1] * p1[l][m - 1];
+          p2[l][m] = p2[l][m - 1] * p2[l][m - 1];
+        }
+#pragma unroll
+      for (int e = 0; e < NE; ++e) {
+        const float E1 = w1 * exa[e] * ex[e * cap + b1];
+        const float E2 = w2 * exa[e] * ex[e * cap + b2];
+#pragma unroll
+        for (int l = 0; l < NL; ++l)
+#pragma unroll
+          for (int m = 0; m < NZ; ++m) acc[e][l][m] = fmaf(p2[l][m], E2, fmaf(p1[l][m], E1, acc[e][l][m]));
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) {
+        const float v = warp_sum(acc[e][l][m]);
+        if (lane == 0) S.scratch[(e * NL + l) * NZ_MAX + m] = v;
+      }
+}
+
+// Chain rule of one block: per triplet phi = dE/dcos and eta0/eta1 = dE/dr_ij, dE/dr_ik
+// summed over the block's functions (BasisA::force, basis_angular.cpp:456-507), turned into the
+// neighbour-slot vectors of NNP::force (nnp.cpp:466-478).  The owner's vector accumulates in
+// registers; the partner's goes to shared memory (distinct partners within a round).
+// One triplet of the chain rule for owner a (registers) and partner b: returns the owner-side
+// vector in (oa*) and the partner-side vector in (ob*).
+template <int NE, int NZ>
+__device__ __forceinline__ void chain_triplet(float uax, float uay, float uaz, float fa, float ga, float pa, float ia, const float* exa,
+                                              float ubx, float uby, float ubz, float fb, float gb, float pb, float ib, const float* exb,
+                                              const float (&sg)[NE][NL][NZ], const float* ie, float lam0, float lam1, float hn, float nn,
+                                              float& oa0, float& oa1, float& oa2, float& ob0, float& ob1, float& ob2) {
+  const float cs = uax * ubx + uay * uby + uaz * ubz;
+  float p[NL][NZ], qd[NL][NZ];
+  p[0][0] = fabsf(0.5f * (1.0f + lam0 * cs));
+  p[1][0] = fabsf(0.5f * (1.0f + lam1 * cs));
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    qd[l][0] = 1.0f;
+#pragma unroll
+    for (int m = 1; m < NZ; ++m) {
+      qd[l][m] = 2.0f * qd[l][m - 1] * p[l][m - 1];
+      p[l][m] = p[l][m - 1] * p[l][m - 1];
+    }
+  }
+  float Q = 0.f, Q2 = 0.f, Pp = 0.f;
+#pragma unroll
+  for (int e = 0; e < NE; ++e) {
+    const float E = exa[e] * exb[e];
+    float q0 = 0.f, q1 = 0.f, r0 = 0.f, r1 = 0.f;
+#pragma unroll
+    for (int m = 0; m < NZ; ++m) {
+      q0 = fmaf(sg[e][0][m], p[0][m], q0);
+      q1 = fmaf(sg[e][1][m], p[1][m], q1);
+      r0 = fmaf(sg[e][0][m], qd[0][m], r0);
+      r1 = fmaf(sg[e][1][m], qd[1][m], r1);
+    }
+    const float qe = q0 + q1;
+    const float pe = lam0 * r0 + lam1 * r1;
+    Q = fmaf(E, qe, Q);
+    Q2 = fmaf(E * ie[e], qe, Q2);
+    Pp = fmaf(E, pe, Pp);
+  }
+  const float phi = hn * fa * fb * Pp;
+  const float eta0 = nn * fb * (ga * Q - pa * Q2);
+  const float eta1 = nn * fa * (gb * Q - pb * Q2);
+  const float Aa = -phi * cs * ia + eta0, Ba = phi * ia;
+  const float Ab = -phi * cs * ib + eta1, Bb = phi * ib;
+  oa0 = Aa * uax + Ba * ubx;
+  oa1 = Aa * uay + Ba * uby;
+  oa2 = Aa * uaz + Ba * ubz;
+  ob0 = Ab * ubx + Bb * uax;
+  ob1 = Ab * uby + Bb * uay;
+  ob2 = Ab * ubz + Bb * uaz;
+}
+
+// Chain rule of one block: per triplet phi = dE/dcos and eta0/eta1 = dE/dr_ij, dE/dr_ik
+// summed over the block's functions (BasisA::force, basis_angular.cpp:456-507), turned into the
+// neighbour-slot vectors of NNP::force (nnp.cpp:466-478).  The owner's vector accumulates in
+// registers; the partner's goes to shared memory (distinct partners within a round).
+template <int NE, int NZ>
+__device__ __forceinline__ void force_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  const int lane = threadIdx.x & 31;
+  float sg[NE][NL][NZ];
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) sg[e][l][m] = S.scratch[(e * NL + l) * NZ_MAX + m];
+  float ie[NE];
+#pragma unroll
+  for (int e = 0; e < NE; ++e) ie[e] = A.ietap[e];
+  const float lam0 = A.lam[0], lam1 = A.lam[1];
+  const float hn = -0.5f * A.norm, nn = -A.norm;
+  const float* __restrict__ ux = S.ux;
+  const float* __restrict__ uy = S.uy;
+  const float* __restrict__ uz = S.uz;
+  const float* __restrict__ ex = S.ex;
+  const float* __restrict__ fc = S.fc;
+  const float* __restrict__ gc = S.gc;
+  const float* __restrict__ dpa = S.dpa;
+  const float* __restrict__ inv = S.inv;
+  float* __restrict__ wx = S.wx;
+  float* __restrict__ wy = S.wy;
+  float* __restrict__ wz = S.wz;
+  for (int q = 0; q * 32 < sc.nown; ++q) {
+    const int x = q * 32 + lane;
+    const int a = sc.xb + min(x, sc.nown - 1);
+    const float uax = ux[a], uay = uy[a], uaz = uz[a];
+    const float fa = fc[a], ga = gc[a], pa = dpa[a], ia = inv[a];
+    float exa[NE];
+#pragma unroll
+    for (int e = 0; e < NE; ++e) exa[e] = ex[e * cap + a];
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    for (int dd = sc.d0; dd <= sc.d1; ++dd) {
+      const int nx = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+      if (x < nx) {
+        int y = x + dd;
+        if (y >= sc.mod) y -= sc.mod;
+        const int b = sc.yb + y;
+        float exb[NE];
+#pragma unroll
+        for (int e = 0; e < NE; ++e) exb[e] = ex[e * cap + b];
+        float a0, a1, a2, c0, c1, c2;
+        chain_triplet<NE, NZ>(uax, uay, uaz, fa, ga, pa, ia, exa, ux[b], uy[b], uz[b], fc[b], gc[b], dpa[b], inv[b], exb, sg, ie, lam0,
+                              lam1, hn, nn, a0, a1, a2, c0, c1, c2);
+        w0 += a0; w1 += a1; w2 += a2;
+        wx[b] += c0; wy[b] += c1; wz[b] += c2;
+      }
+      __syncwarp();
+    }
+    if (x < sc.nown) {
+      wx[sc.xb + x] += w0;
+      wy[sc.xb + x] += w1;
+      wz[sc.xb + x] += w2;
+    }
+    __syncwarp();
+  }
+}
+
+// Dispatch on the block's grid size: eta count 1..NEK, zeta chain length rounded up to 3, 5 or 6
+// (at most NZK).  Only instances within the kernel's bounds are linked, which keeps the
+// kernel's register allocation to what its potential needs.
+template <bool FORCE, int NEK, int NZK>
+__device__ void run_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  const int z = A.nz <= 3 ? 3 : (A.nz <= 5 ? 5 : 6);
+  const int key = A.ne * 8 + z;
+#define NNP_CASE(NE_, NZ_)                                   \
+  case NE_ * 8 + NZ_:                                        \
+    if constexpr (NE_ <= NEK && NZ_ <= NZK) {                \
+      if (FORCE) force_block<NE_, NZ_>(S, A, sc, cap);       \
+      else symm_block<NE_, NZ_>(S, A, sc, cap);              \
+    }                                                        \
+    break;
+  switch (key) {
+    NNP_CASE(1, 3) NNP_CASE(1, 5) NNP_CASE(1, 6)
+    NNP_CASE(2, 3) NNP_CASE(2, 5) NNP_CASE(2, 6)
+    NNP_CASE(3, 3) NNP_CASE(3, 5) NNP_CASE(3, 6)
+    NNP_CASE(4, 3) NNP_CASE(4, 5) NNP_CASE(4, 6)
+    default: break;
+  }
+#undef NNP_CASE
+}
+
+// ------------------------------------------------------------------------------------ symm
+template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                    const int* __restrict__ type, const int* __restrict__ nb_j,
                                                    const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt,
@@ -123,7 +354,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
-  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NE), cap, NE);
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
   const int I = clamp_type(type[i], P.ntypes);
   stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
   float* Gi = G + (size_t)i * gstride;
@@ -154,7 +385,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       }
   }
 
-  // ---- angular blocks (J <= K): G4 (BasisA::symm, basis_angular.cpp:406-421)
+  // ---- angular blocks (J <= K): G4
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
@@ -164,61 +395,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       block_pair_factors(S, A, j0, j0 + nJ, cap, true);
       if (K != J) block_pair_factors(S, A, k0, k0 + nK, cap, true);
       __syncwarp();
-      float acc[NE][NL][NZ];
-#pragma unroll
-      for (int e = 0; e < NE; ++e)
-#pragma unroll
-        for (int l = 0; l < NL; ++l)
-#pragma unroll
-          for (int m = 0; m < NZ; ++m) acc[e][l][m] = 0.f;
-      const bool tri = (J == K);
-      int xb, nown, yb, mod, d0, d1;
-      if (tri) { xb = j0; yb = j0; nown = nJ; mod = nJ; d0 = 1; d1 = nJ / 2; }
-      else if (nJ <= nK) { xb = j0; nown = nJ; yb = k0; mod = nK; d0 = 0; d1 = nK - 1; }
-      else { xb = k0; nown = nK; yb = j0; mod = nJ; d0 = 0; d1 = nJ - 1; }
-      if (nown == 0) d1 = d0 - 1;
-      const float lam0 = A.lam[0], lam1 = A.lam[1];
-      for (int dd = d0; dd <= d1; ++dd) {
-        const int nx = (tri && 2 * dd == nJ) ? (nJ >> 1) : nown;
-#pragma unroll
-        for (int q = 0; q < QMAX; ++q) {
-          if (q * 32 >= nx) break;
-          const int x = q * 32 + lane;
-          if (x < nx) {
-            int y = x + dd;
-            if (y >= mod) y -= mod;
-            const int a = xb + x, b = yb + y;
-            const float cs = S.ux[a] * S.ux[b] + S.uy[a] * S.uy[b] + S.uz[a] * S.uz[b];
-            float p[NL][NZ];
-#pragma unroll
-            for (int l = 0; l < NL; ++l) {
-              p[l][0] = fabsf(0.5f * (1.0f + (l == 0 ? lam0 : lam1) * cs));
-#pragma unroll
-              for (int m = 1; m < NZ; ++m) p[l][m] = p[l][m - 1] * p[l][m - 1];
-            }
-#pragma unroll
-            for (int e = 0; e < NE; ++e)
-              if (e < A.ne) {
-                const float E = S.ex[e * cap + a] * S.ex[e * cap + b];
-#pragma unroll
-                for (int l = 0; l < NL; ++l)
-#pragma unroll
-                  for (int m = 0; m < NZ; ++m)
-                    if (m < A.nz) acc[e][l][m] = fmaf(p[l][m], E, acc[e][l][m]);
-              }
-          }
-        }
-      }
-      // reduce the grid and scatter it to the block's file functions
-#pragma unroll
-      for (int e = 0; e < NE; ++e)
-#pragma unroll
-        for (int l = 0; l < NL; ++l)
-#pragma unroll
-          for (int m = 0; m < NZ; ++m) {
-            const float v = warp_sum(acc[e][l][m]);
-            if (lane == 0) S.scratch[(e * NL + l) * NZ_MAX + m] = v;
-          }
+      run_block<false, NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
       for (int f = lane; f < A.n; f += 32) Gi[A.off + f] = A.norm * S.scratch[A.gidx[f]];
       __syncwarp();
@@ -226,7 +403,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
 }
 
 // ------------------------------------------------------------------------------------ force
-template <int NE, int NZ>
+template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
                                                     const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt,
@@ -235,7 +412,7 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
-  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NE), cap, NE);
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
   const int I = clamp_type(type[i], P.ntypes);
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
   const float* gi = dEdG + (size_t)i * gstride;
@@ -265,7 +442,7 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   }
   __syncwarp();
 
-  // ---- angular chain rule (BasisA::force, basis_angular.cpp:456-507; nnp.cpp:448-479)
+  // ---- angular chain rule
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
@@ -281,98 +458,7 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
         for (int f = 0; f < A.n; ++f) S.scratch[A.gidx[f]] += gi[A.off + f];
       }
       __syncwarp();
-      float sg[NE][NL][NZ];
-#pragma unroll
-      for (int e = 0; e < NE; ++e)
-#pragma unroll
-        for (int l = 0; l < NL; ++l)
-#pragma unroll
-          for (int m = 0; m < NZ; ++m) sg[e][l][m] = S.scratch[(e * NL + l) * NZ_MAX + m];
-      float ie[NE];
-#pragma unroll
-      for (int e = 0; e < NE; ++e) ie[e] = (e < A.ne) ? A.ietap[e] : 0.f;
-      const float lam0 = A.lam[0], lam1 = A.lam[1];
-      const float hn = -0.5f * A.norm, nn = -A.norm;
-
-      const bool tri = (J == K);
-      int xb, nown, yb, mod, d0, d1;
-      if (tri) { xb = j0; yb = j0; nown = nJ; mod = nJ; d0 = 1; d1 = nJ / 2; }
-      else if (nJ <= nK) { xb = j0; nown = nJ; yb = k0; mod = nK; d0 = 0; d1 = nK - 1; }
-      else { xb = k0; nown = nK; yb = j0; mod = nJ; d0 = 0; d1 = nJ - 1; }
-      float wo[QMAX][3];
-#pragma unroll
-      for (int q = 0; q < QMAX; ++q) wo[q][0] = wo[q][1] = wo[q][2] = 0.f;
-      for (int dd = d0; dd <= d1; ++dd) {
-        const int nx = (tri && 2 * dd == nJ) ? (nJ >> 1) : nown;
-#pragma unroll
-        for (int q = 0; q < QMAX; ++q) {
-          if (q * 32 >= nx) break;
-          const int x = q * 32 + lane;
-          if (x < nx) {
-            int y = x + dd;
-            if (y >= mod) y -= mod;
-            const int a = xb + x, b = yb + y;
-            const float uax = S.ux[a], uay = S.uy[a], uaz = S.uz[a];
-            const float ubx = S.ux[b], uby = S.uy[b], ubz = S.uz[b];
-            const float cs = uax * ubx + uay * uby + uaz * ubz;
-            float p[NL][NZ], qd[NL][NZ];
-#pragma unroll
-            for (int l = 0; l < NL; ++l) {
-              p[l][0] = fabsf(0.5f * (1.0f + (l == 0 ? lam0 : lam1) * cs));
-              qd[l][0] = 1.0f;
-#pragma unroll
-              for (int m = 1; m < NZ; ++m) {
-                qd[l][m] = 2.0f * qd[l][m - 1] * p[l][m - 1];
-                p[l][m] = p[l][m - 1] * p[l][m - 1];
-              }
-            }
-            float Q = 0.f, Q2 = 0.f, Pp = 0.f;
-#pragma unroll
-            for (int e = 0; e < NE; ++e)
-              if (e < A.ne) {
-                const float E = S.ex[e * cap + a] * S.ex[e * cap + b];
-                float qe = 0.f, pe = 0.f;
-#pragma unroll
-                for (int l = 0; l < NL; ++l) {
-                  float ql = 0.f, pl = 0.f;
-#pragma unroll
-                  for (int m = 0; m < NZ; ++m) {
-                    ql = fmaf(sg[e][l][m], p[l][m], ql);
-                    pl = fmaf(sg[e][l][m], qd[l][m], pl);
-                  }
-                  qe += ql;
-                  pe = fmaf(l == 0 ? lam0 : lam1, pl, pe);
-                }
-                Q = fmaf(E, qe, Q);
-                Q2 = fmaf(E * ie[e], qe, Q2);
-                Pp = fmaf(E, pe, Pp);
-              }
-            const float fa = S.fc[a], fb = S.fc[b];
-            const float phi = hn * fa * fb * Pp;
-            const float eta0 = nn * fb * (S.gc[a] * Q - S.dpa[a] * Q2);
-            const float eta1 = nn * fa * (S.gc[b] * Q - S.dpa[b] * Q2);
-            const float ia = S.inv[a], ib = S.inv[b];
-            const float Aa = -phi * cs * ia + eta0, Ba = phi * ia;
-            const float Ab = -phi * cs * ib + eta1, Bb = phi * ib;
-            wo[q][0] += Aa * uax + Ba * ubx;
-            wo[q][1] += Aa * uay + Ba * uby;
-            wo[q][2] += Aa * uaz + Ba * ubz;
-            S.wx[b] += Ab * ubx + Bb * uax;
-            S.wy[b] += Ab * uby + Bb * uay;
-            S.wz[b] += Ab * ubz + Bb * uaz;
-          }
-          __syncwarp();
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < QMAX; ++q) {
-        const int x = q * 32 + lane;
-        if (x < nown) {
-          S.wx[xb + x] += wo[q][0];
-          S.wy[xb + x] += wo[q][1];
-          S.wz[xb + x] += wo[q][2];
-        }
-      }
+      run_block<true, NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
     }
 
@@ -384,45 +470,43 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
 size_t symm_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne) * warps; }
 size_t force_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne) * warps; }
 
-template <int NE, int NZ>
-static int launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
-  const size_t smem = symm_smem_bytes(B.cap, NE, warps);
+template <int NEK, int NZK>
+static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(symm_kernel<NE, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(symm_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  symm_kernel<NE, NZ><<<(B.natoms + warps - 1) / warps, 32 * warps, smem, st>>>(P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r,
-                                                                                  B.nb_cnt, B.G, B.gstride);
-  return 0;
+  symm_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.G, B.gstride);
 }
-template <int NE, int NZ>
-static int launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
-  const size_t smem = force_smem_bytes(B.cap, NE, warps);
+template <int NEK, int NZK>
+static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(force_kernel<NE, NZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(force_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     attr = true;
   }
-  force_kernel<NE, NZ><<<(B.natoms + warps - 1) / warps, 32 * warps, smem, st>>>(P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r,
-                                                                                   B.nb_cnt, B.dEdG, B.gstride, B.W);
-  return 0;
+  force_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps), st>>>(
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.W);
 }
 
-// Template instance covering (ne, nz): ne in {2,4}, nz in {5,6}.
+// Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).
 int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st) {
   if (B.natoms == 0) return 0;
-  if (ne <= 2 && nz <= 5) return launch_symm_t<2, 5>(B, P, warps, st);
-  if (ne <= 4 && nz <= 5) return launch_symm_t<4, 5>(B, P, warps, st);
-  if (ne <= 4 && nz <= 6) return launch_symm_t<4, 6>(B, P, warps, st);
-  return -1;
+  if (ne <= 2 && nz <= 5) launch_symm_t<2, 5>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 5) launch_symm_t<4, 5>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 6) launch_symm_t<4, 6>(B, P, warps, st);
+  else return -1;
+  return 0;
 }
 int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st) {
   if (B.natoms == 0) return 0;
-  if (ne <= 2 && nz <= 5) return launch_force_t<2, 5>(B, P, warps, st);
-  if (ne <= 4 && nz <= 5) return launch_force_t<4, 5>(B, P, warps, st);
-  if (ne <= 4 && nz <= 6) return launch_force_t<4, 6>(B, P, warps, st);
-  return -1;
+  if (ne <= 2 && nz <= 5) launch_force_t<2, 5>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 5) launch_force_t<4, 5>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 6) launch_force_t<4, 6>(B, P, warps, st);
+  else return -1;
+  return 0;
 }
 
 }  // namespace nnpgpu
