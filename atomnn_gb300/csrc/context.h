@@ -44,8 +44,9 @@ struct nnpgpu_ctx {
   nnpgpu::NetsP nets{};
   void* netbuf = nullptr;
   size_t netbytes = 0;
-  void* tcbuf = nullptr;  // BF16 weights of the tensor-core path
+  void* tcbuf = nullptr;  // BF16 weights of the tensor-core path (packed operand layout)
   size_t tcbytes = 0;
+  std::shared_ptr<std::vector<uint8_t>> tcnets;  // kernel parameter block of that path
   size_t budget = 0, used = 0;
   int cap_hint = 0;
   nnpgpu::TuneCfg tune;

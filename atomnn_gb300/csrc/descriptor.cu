@@ -473,20 +473,14 @@ size_t force_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * war
 template <int NEK, int NZK>
 static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(symm_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   symm_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.G, B.gstride);
 }
 template <int NEK, int NZK>
 static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(force_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   force_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps), st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.W);
 }

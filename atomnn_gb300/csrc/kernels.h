@@ -61,7 +61,8 @@ size_t force_smem_bytes(int cap, int ne, int warps);
 // atomic networks: FP32 SIMT path and BF16 tensor-core path
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st);
 void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile, cudaStream_t st);
-int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weights, int ntypes, cudaStream_t st);
+int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weights, int ntypes, cudaStream_t st, const void* tcnets_host,
+                        int want_grad);
 // force gather, orphan fix-up, per-structure energy
 void launch_gather(const BatchDev& B, const NetsP& N, bool add_vacuum, bool want_force, cudaStream_t st);
 

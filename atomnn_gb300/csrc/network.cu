@@ -187,10 +187,7 @@ void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int /*ti
     floats = max(floats, f);
   }
   static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(network_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr = true;
-  }
+  if (!attr) attr = cudaFuncSetAttribute(network_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   const int tiles = (B.natoms + TILE - 1) / TILE + ntypes;
   network_fp32_kernel<<<tiles, 128, floats * sizeof(float), st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride, B.eatom,
                                                                    B.dEdG, 1);

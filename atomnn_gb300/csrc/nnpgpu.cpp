@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
@@ -181,8 +182,10 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
   if (want_energy || want_force) {
     launch_type_sort(B, c->pot.ntypes, st);
     if (flags & NNPGPU_BF16) {
-      const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st);
-      if (rcode != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "BF16 network path unavailable for this potential");
+      const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st, c->tcnets ? c->tcnets->data() : nullptr,
+                                            want_force ? 1 : 0);
+      if (rcode == -1) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "BF16 network path unavailable for this potential");
+      if (rcode != 0) return cuda_fail(c, cudaGetLastError(), "tensor-core network set-up");
     } else {
       launch_network_fp32(B, c->nets, c->pot.ntypes, c->tune.nn_tile, st);
     }
@@ -357,8 +360,14 @@ void drop_graphs(nnpgpu_ctx* c) {
 // Reads the status words after the stream finished; returns OK, a retry request (>0 = new
 // capacity) or an error.
 int check_status(nnpgpu_ctx* c, const int* st_words, int cap) {
+  if (getenv("NNPGPU_DEBUG")) {
+    std::fprintf(stderr, "nnpgpu status:");
+    for (int k = 0; k < ST_WORDS; ++k) std::fprintf(stderr, " %d", st_words[k]);
+    std::fprintf(stderr, "\n");
+  }
   if (st_words[ST_ERROR] & ERR_BAD_POSITION) return set_error(c, NNPGPU_ERR_INVALID, "non-finite atom position");
   if (st_words[ST_ERROR] & ERR_BAD_TYPE) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
+  if (st_words[ST_ERROR] & ERR_TIMEOUT) return set_error(c, NNPGPU_ERR_TIMEOUT, "a bounded wait on the device ran out (tensor-core network)");
   if (st_words[ST_ERROR] & ERR_ORPHANS) return set_error(c, NNPGPU_ERR_INVALID, "inconsistent neighbour lists (too many unmatched minimum images)");
   if (st_words[ST_MAXCOUNT] > cap) {
     const int need = (st_words[ST_MAXCOUNT] + 31) / 32 * 32;

@@ -201,3 +201,31 @@ def test_full_size_properties(engines):
     assert abs(es[0] / sup.natoms - ec[0] / c.natoms) < E_TOL
     for r in range(8):
         assert np.abs(Fs[0][r * 1728:(r + 1) * 1728] - Fc[0]).max() < F_TOL
+
+
+# ---- BF16 tensor-core networks: the spec gate is force RMSE <= 1e-3 eV/A against the
+# FP64 oracle; the energy per atom is held to 1e-3 eV/atom.
+BF16_F_RMSE = 1e-3
+BF16_E_TOL = 1e-3
+
+
+@pytest.mark.parametrize("name", ["small64", "mixed3"])
+def test_bf16_networks_against_golden(engines, name):
+    pot = str(np.load(os.path.join(GOLDEN, name + ".npz"))["potential"][0])
+    cases = load_golden(name)
+    e, F, _ = engines[pot].compute([s for s, _ in cases], _flags("ENERGY", "FORCE", "BATCHED", "BF16"))
+    for k, (s, ref) in enumerate(cases):
+        assert abs(e[k] - ref["energy"][0]) / s.natoms <= BF16_E_TOL
+        assert np.sqrt(((F[k] - ref["force"]) ** 2).mean()) <= BF16_F_RMSE
+
+
+def test_bf16_networks_mixed_batch(engines, oracles):
+    strucs = W.make_structures("mixed512", seed=12, count=6, sizes=[16, 50, 130, 400, 900, 1500])
+    e, F, _ = engines["mixed512"].compute(strucs, _flags("ENERGY", "FORCE", "BATCHED", "BF16"))
+    e32, F32, _ = engines["mixed512"].compute(strucs, _flags("ENERGY", "FORCE", "BATCHED"))
+    for k, s in enumerate(strucs):
+        eo, Fo, _ = oracles["mixed512"].compute(s.posn, s.species, s.cell, force=True)
+        assert abs(e[k] - eo) / s.natoms <= BF16_E_TOL
+        assert np.sqrt(((F[k] - Fo) ** 2).mean()) <= BF16_F_RMSE
+        # and the BF16 path really differs from the FP32 one (the tensor-core kernel ran)
+        assert not np.array_equal(F[k], F32[k])
