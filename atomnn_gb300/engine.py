@@ -18,7 +18,7 @@ ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
-           "nnpgpu_profile_stage_name"]
+           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc"]
 
 _lib = None
 
@@ -69,6 +69,7 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_profile_read.argtypes = [vp, ip, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_longlong)]
     L.nnpgpu_profile_stage_name.argtypes = [ip]
     L.nnpgpu_profile_stage_name.restype = cp
+    L.nnpgpu_symm_noalloc.argtypes = [vp, ip, vp, vp, vp, vp, ip, vp]
     _lib = L
     return L
 
@@ -148,6 +149,13 @@ class Engine:
                                                    ctypes.c_void_p(d_species), _p(cells), flags, ctypes.c_void_p(d_energy or None),
                                                    ctypes.c_void_p(d_force or None), ctypes.c_void_p(d_symm or None),
                                                    ctypes.c_void_p(stream or None)))
+
+    def symm_noalloc(self, natoms, d_posn, d_species, cell, d_symm, symm_stride, stream=0):
+        """nnpgpu_symm_noalloc: symmetry functions of one structure with no device allocation
+        (device pointers in and out; cell is a 3x3 host array, columns = lattice vectors)."""
+        cellc = _cell_colmajor(cell)
+        self._check(self.lib.nnpgpu_symm_noalloc(self._ctx, natoms, ctypes.c_void_p(d_posn or None), ctypes.c_void_p(d_species or None),
+                                                 _p(cellc), ctypes.c_void_p(d_symm or None), symm_stride, ctypes.c_void_p(stream or None)))
 
     def profile_enable(self, on=True):
         self._check(self.lib.nnpgpu_profile_enable(self._ctx, 1 if on else 0))

@@ -90,6 +90,22 @@ int nnpgpu_compute_device(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const 
 int nnpgpu_neighbors(nnpgpu_ctx* ctx, int natoms, const double* posn, const double* cell, int cap,
                      int* count, int* index, float* r, unsigned char* min, int* shift);
 
+/* ---- symmetry functions without device allocation.  No counterpart in the reference (AtomNN
+ * allocates through Eigen on every call).  For callers that cannot let a library allocate device
+ * memory while they run: codes that divide the GPU's memory among their own pools before the
+ * first step, and services that reserve all device memory at start-up.  Computes NNP::symm
+ * (src/nnp/nnp.cpp:334-381) of one structure of at most 1024 atoms with at most 192 neighbours per
+ * atom and 512 lattice images, keeping every intermediate in a 4.6 MB scratch array compiled into
+ * the library (each GPU that loads the library holds it until the process exits).
+ * d_posn (natoms*3 FP64), d_species and d_symm (natoms rows of symm_stride FP32, symm_stride >= the
+ * largest nnpgpu_ninput) are device pointers; cell is a host array as in nnpgpu_compute.  Returns
+ * after the work on stream (NULL = the context's stream) has finished.  Larger requests are
+ * rejected with NNPGPU_ERR_INVALID or NNPGPU_ERR_CAPACITY and a message.  The first call on a
+ * device looks up the scratch array's address: make that call before any stream capture.  All
+ * calls share the scratch array, so calls whose work overlaps on the GPU race on it. */
+int nnpgpu_symm_noalloc(nnpgpu_ctx* ctx, int natoms, const double* d_posn, const int* d_species, const double* cell,
+                        float* d_symm, int symm_stride, void* stream);
+
 /* ---- stage tracing (diagnostics; the reference times phases with util/Clock, e.g.
  * src/nnp/nnpte.cpp:1971-1990).  When enabled, CUDA events bracket each stage of the batched
  * launch sequence and their durations accumulate per stage.  Enabling resets the counters. */
