@@ -68,10 +68,16 @@ struct NetsP {
 };
 
 // Per-structure geometry of a batch.  mode: 0 non-periodic, 1 image shells (some shell > 0),
-// 2 single image (all shells 0: at most one image of each atom within the cutoff).
+// 2 single image (all shells 0: at most one image of each atom within the cutoff), 3 single
+// image with the candidate pairs taken from a resident skin list (skin_j/skin_code/skin_cnt,
+// local atom indices, skin_cap slots per atom) instead of all atoms of the structure.
 struct StrucMeta {
   int atom0, natoms, mode, nimg;
-  int img0, pad0, pad1, pad2;
+  int img0, skin_cap, pad1, pad2;
+  const int* skin_j;
+  const int* skin_code;
+  const int* skin_cnt;
+  const void* pad3;
   double R[9], RInv[9];  // column-major
   double dMax2, fro;
   double shifts[18];     // +col0, -col0, +col1, -col1, +col2, -col2 (Cell::init, src/struc/cell.cpp:63-69)

@@ -31,10 +31,20 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
 
 class Serving;
 
+// A resident neighbour list (built with cutoff rc + skin) that a structure of a batch may use
+// instead of searching all atoms (neighbour mode 3); j/code/cnt are device arrays, cap slots per atom.
+struct SkinRef {
+  const int* j = nullptr;
+  const int* code = nullptr;
+  const int* cnt = nullptr;
+  int cap = 0;
+};
+
 }  // namespace nnpgpu
 
 struct nnpgpu_ctx {
   std::string err;
+  std::string potfile;
   int device = 0;
   int verbose = 0;
   cudaStream_t stream = nullptr;
@@ -74,6 +84,14 @@ bool ensure_host(nnpgpu_ctx* c, HostBuf& b, size_t bytes);
 // Runs the launch sequence for atoms of structures [s0, s0+ns) of the uploaded batch.
 int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st);
 int set_error(nnpgpu_ctx* c, int code, const std::string& msg);
+// Host-buffer batch evaluation with optional resident skin lists per structure (skins may be null;
+// an entry with cnt == nullptr, or a structure that is not single-image at rc, builds normally).
+int compute_host(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell, int flags,
+                 double* energy, double* force, float* symm, const SkinRef* skins);
+// Builds the neighbour list of one structure with cutoff rc_skin into device arrays of skin_cap
+// slots per atom (local atom indices).  Returns OK, or NNPGPU_ERR_CAPACITY with *max_count set.
+int build_skin(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, double rc_skin, int skin_cap, int* d_j, int* d_code,
+               int* d_cnt, float4* d_r, int* max_count);
 // Packs the BF16 weights of the tensor-core network path (network_tc.cu).
 int prepare_tc_weights(nnpgpu_ctx* c);
 }  // namespace nnpgpu

@@ -164,6 +164,54 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc);
       count += __popc(mk);
     }
+  } else if (S.mode == 3) {
+    // resident skin list (built with a larger cutoff at some earlier positions): the candidates
+    // are its (j, T) entries in their stored order (j ascending); each is re-decided exactly as
+    // in mode 2 for the current positions.
+    const float4 si = sfrac[i];
+    const int4 fi = sfloor[i];
+    const int il = i - j0;
+    const int ns = S.skin_cnt[il];
+    const int* sj_l = S.skin_j + (size_t)il * S.skin_cap;
+    const int* sc_l = S.skin_code + (size_t)il * S.skin_cap;
+    for (int c = 0; c < ns; c += 32) {
+      const int s = c + lane;
+      bool keep = false;
+      float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
+      int T[3] = {0, 0, 0};
+      int j = -1;
+      if (s < ns) {
+        const int jl = sj_l[s];
+        const int code = sc_l[s];
+        T[0] = code_t(code, 0);
+        T[1] = code_t(code, 1);
+        T[2] = code_t(code, 2);
+        j = j0 + jl;
+        const float4 sj = sfrac[j];
+        const int4 fj = sfloor[j];
+        // f_i - f_j - T = (s_i - s_j) + (floor_i - floor_j - T): the integer part is exact
+        const float d0 = (si.x - sj.x) + (float)(fi.x - fj.x - T[0]);
+        const float d1 = (si.y - sj.y) + (float)(fi.y - fj.y - T[1]);
+        const float d2 = (si.z - sj.z) + (float)(fi.z - fj.z - T[2]);
+        rf_mul(S, d0, d1, d2, r0, r1, r2);
+        const float d2f = r0 * r0 + r1 * r1 + r2 * r2;
+        if (d2f < rc2f - m) {
+          keep = true;
+          dr = sqrtf(d2f);
+        } else if (d2f <= rc2f + m) {
+          double o0, o1, o2;
+          int D[3];
+          cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], o0, o1, o2, D);
+          const double dd = sqn3(o0, o1, o2);
+          keep = (D[0] == T[0] && D[1] == T[1] && D[2] == T[2]) && dd <= rc2;
+          r0 = (float)o0; r1 = (float)o1; r2 = (float)o2;
+          dr = (float)sqrt(dd);
+        }
+      }
+      const unsigned mk = __ballot_sync(0xffffffffu, keep);
+      if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(T[0], T[1], T[2], true), oj, orr, oc);
+      count += __popc(mk);
+    }
   } else if (S.mode == 1) {
     // image shells: for each j, every shift of the box around the Cell::diff image (reference order)
     const ImgEntry* im = imgs + S.img0;

@@ -216,7 +216,8 @@ struct Uploaded {
 };
 
 // Validates the batch description and uploads geometry metadata; sizes all batch buffers.
-int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, int cap, Uploaded& U, cudaStream_t st) {
+int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, int cap, Uploaded& U, cudaStream_t st,
+            const SkinRef* skins = nullptr) {
   if (nstruc < 0 || (nstruc > 0 && (!natoms || !cell))) return set_error(c, NNPGPU_ERR_INVALID, "invalid batch description");
   U.nstruc = nstruc;
   U.offsets.assign(nstruc + 1, 0);
@@ -228,7 +229,16 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
   std::vector<ImgEntry> imgs;
   U.metas.resize(nstruc);
   try {
-    for (int s = 0; s < nstruc; ++s) make_meta(cell + 9 * s, U.offsets[s], natoms[s], c->pot.rc, U.metas[s], imgs);
+    for (int s = 0; s < nstruc; ++s) {
+      make_meta(cell + 9 * s, U.offsets[s], natoms[s], c->pot.rc, U.metas[s], imgs);
+      if (skins && skins[s].cnt && U.metas[s].mode == 2) {
+        U.metas[s].mode = 3;
+        U.metas[s].skin_j = skins[s].j;
+        U.metas[s].skin_code = skins[s].code;
+        U.metas[s].skin_cnt = skins[s].cnt;
+        U.metas[s].skin_cap = skins[s].cap;
+      }
+    }
   } catch (PotError& e) {
     return set_error(c, e.code, e.what());
   }
@@ -390,6 +400,7 @@ extern "C" int nnpgpu_create(const char* potfile, const nnpgpu_opts* opts, nnpgp
     c->budget = opts ? opts->hbm_budget_bytes : 0;
     c->cap_hint = opts ? opts->max_neighbors : 0;
     if (!potfile) throw PotError(NNPGPU_ERR_INVALID, "no potential file");
+    c->potfile = potfile;
     c->pot = read_potential(potfile);
     build_tables(c->pot, c->P, c->ne, c->nz);
     c->max_nin = 0;
@@ -530,7 +541,8 @@ extern "C" int nnpgpu_ninput(const nnpgpu_ctx* c, int type) {
 }
 
 static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
-                        int flags, double* energy, double* force, float* symm, bool device_io, cudaStream_t st) {
+                        int flags, double* energy, double* force, float* symm, bool device_io, cudaStream_t st,
+                        const SkinRef* skins = nullptr) {
   if (!c) return NNPGPU_ERR_INVALID;
   if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
   cudaSetDevice(c->device);
@@ -547,7 +559,7 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
   int cap = estimate_cap(c, nstruc, natoms, cell);
   for (int attempt = 0; attempt < 4; ++attempt) {
     Uploaded U;
-    int rc = prepare(c, nstruc, natoms, cell, cap, U, st);
+    int rc = prepare(c, nstruc, natoms, cell, cap, U, st, skins);
     if (rc != NNPGPU_OK) return rc;
     const size_t N = total;
     const double* dposn = posn;
@@ -606,6 +618,45 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
   }
   return set_error(c, NNPGPU_ERR_CAPACITY, "neighbour capacity retries exhausted");
 }
+
+namespace nnpgpu {
+int compute_host(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell, int flags,
+                 double* energy, double* force, float* symm, const SkinRef* skins) {
+  return compute_impl(c, nstruc, natoms, posn, species, cell, flags, energy, force, symm, false, nullptr, skins);
+}
+
+int build_skin(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, double rc_skin, int skin_cap, int* d_j, int* d_code,
+               int* d_cnt, float4* d_r, int* max_count) {
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  *max_count = 0;
+  Uploaded U;
+  // geometry for the larger cutoff (shells follow rc_skin); buffers sized for this structure
+  const double saved = c->pot.rc;
+  c->pot.rc = rc_skin;
+  int rc = prepare(c, 1, &natoms, cell, skin_cap, U, st);
+  c->pot.rc = saved;
+  if (rc != NNPGPU_OK) return rc;
+  cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, st);
+  BatchDev B = batch_view(c, U, (const double*)c->posn.p, nullptr, (double*)c->energy.p, (double*)c->force.p);
+  B.rc = rc_skin;
+  B.nb_j = d_j;
+  B.nb_code = d_code;
+  B.nb_cnt = d_cnt;
+  B.nb_r = d_r;
+  launch_neighbors(B, st);
+  int hstat[ST_WORDS];
+  cudaMemcpyAsync(hstat, c->status.p, sizeof(hstat), cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "skin list");
+  if (hstat[ST_ERROR]) return set_error(c, NNPGPU_ERR_INVALID, "invalid positions in a resident structure");
+  if (hstat[ST_MAXCOUNT] > skin_cap) {
+    *max_count = hstat[ST_MAXCOUNT];
+    return NNPGPU_ERR_CAPACITY;
+  }
+  return NNPGPU_OK;
+}
+}  // namespace nnpgpu
 
 extern "C" int nnpgpu_compute(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
                               int flags, double* energy, double* force, float* symm) {

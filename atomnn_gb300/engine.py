@@ -157,6 +157,33 @@ class Engine:
         self._check(self.lib.nnpgpu_symm_noalloc(self._ctx, natoms, ctypes.c_void_p(d_posn or None), ctypes.c_void_p(d_species or None),
                                                  _p(cellc), ctypes.c_void_p(d_symm or None), symm_stride, ctypes.c_void_p(stream or None)))
 
+    # ---- serving (continuous batching)
+    def serve_start(self, max_batch_atoms=0, max_inflight=2, hbm_budget_bytes=0, skin=1.0, flags=0):
+        o = ServeOpts(max_batch_atoms, max_inflight, hbm_budget_bytes, skin, flags)
+        self._check(self.lib.nnpgpu_serve_start(self._ctx, ctypes.byref(o)))
+
+    def submit(self, struc, key=-1):
+        posn = np.ascontiguousarray(struc.posn, dtype=np.float64)
+        species = np.ascontiguousarray(struc.species, dtype=np.int32)
+        rid = ctypes.c_longlong()
+        self._check(self.lib.nnpgpu_submit(self._ctx, posn.shape[0], _p(posn), _p(species), _p(_cell_colmajor(struc.cell)), key,
+                                           ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, rid, natoms):
+        """(energy, forces, latency_s) when done, None while pending."""
+        e = np.zeros(1)
+        F = np.zeros((natoms, 3))
+        lat = ctypes.c_double()
+        rc = self.lib.nnpgpu_poll(self._ctx, rid, _p(e), _p(F), ctypes.byref(lat))
+        if rc == ERR_BUSY:
+            return None
+        self._check(rc)
+        return float(e[0]), F, lat.value
+
+    def serve_stop(self):
+        self._check(self.lib.nnpgpu_serve_stop(self._ctx))
+
     def profile_enable(self, on=True):
         self._check(self.lib.nnpgpu_profile_enable(self._ctx, 1 if on else 0))
 

@@ -208,6 +208,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-step-atoms", type=int, default=0)
     ap.add_argument("--count", type=int, default=512, help="structures of the workload (512 = the full workload)")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_info()
@@ -321,6 +324,27 @@ def main():
         e2e_t.append(time.perf_counter() - t0)
     barrier()
     e2e_step = statistics.mean(e2e_t)
+
+    # serving: Poisson stream of 16-4096-atom requests with 20% resident MD-style repeat steps,
+    # then a saturating burst; latencies are measured by the engine (submission -> completion)
+    serve_out = None
+    if not args.no_serving:
+        from atomnn_gb300 import serving as SV
+        pool = SV.make_pool()
+        eng.serve_start(max_inflight=3, skin=1.0, flags=(E.BF16 if bf16_ok else 0), hbm_budget_bytes=40 << 30)
+        SV.run_stream(eng, pool, rate=args.serve_rate, duration=1.0, seed=1)
+        st = SV.run_stream(eng, pool, rate=args.serve_rate, duration=args.serve_seconds, seed=2)
+        bu = SV.run_stream(eng, pool, rate=2000.0, duration=1.0, burst=True, repeat_frac=0.0, seed=3)
+        eng.serve_stop()
+        pct = lambda a, q: float(np.percentile(a, q) * 1000.0) if len(a) else None
+        serve_out = {
+            "offered_req_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": st["requests"], "repeat_steps": st["repeats"],
+            "p50_ms": pct(st["latencies"], 50), "p99_ms": pct(st["latencies"], 99), "atoms_per_s": st["atoms"] / st["wall"],
+            "saturated": {"requests": bu["requests"], "atoms_per_s": bu["atoms"] / bu["wall"], "p50_ms": pct(bu["latencies"], 50),
+                          "p99_ms": pct(bu["latencies"], 99)},
+            "desc": "nnpgpu_serve_*: 3 slots, continuous batching, 40 GB admission budget, 1.0 A skin for resident keys, "
+                    "sizes log-uniform 16-4096 atoms",
+        }
     h2d = posn.nbytes + species.nbytes + cells.nbytes + natoms.nbytes
     d2h = 8 * len(strucs) + 24 * total_atoms + 32
 
@@ -381,7 +405,10 @@ def main():
                       "desc": "one structure at a time (12 launches per structure), FP32 networks"},
             "batched_fp32": {"value": total_atoms / (statistics.mean(fp32_ms) / 1000), "unit": "atoms/s", "ms_per_step": statistics.mean(fp32_ms)},
             "accuracy_vs_fp64_oracle": acc,
+            "serving": serve_out,
         }
+        if serve_out is not None and out["plain"]["value"] > 0:
+            serve_out["saturated_vs_plain"] = serve_out["saturated"]["atoms_per_s"] / out["plain"]["value"]
         if cpu is not None:
             out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         print(json.dumps(out), flush=True)

@@ -1,0 +1,87 @@
+"""Serving (continuous batching) on the GPU: a request's result is the same alone and in a mix
+of concurrent requests, resident MD-style repeat steps equal a fresh evaluation, and requests
+beyond the device budget are refused."""
+import os
+import time
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from atomnn_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+E_TOL = 1e-5   # eV/atom
+F_TOL = 1e-4   # eV/A
+
+
+def _wait(eng, rid, natoms, timeout=60.0):
+    t0 = time.time()
+    while time.time() - t0 < timeout:
+        r = eng.poll(rid, natoms)
+        if r is not None:
+            return r
+        time.sleep(0.0005)
+    raise TimeoutError("request %d not served" % rid)
+
+
+@pytest.fixture
+def served(native_lib):
+    from atomnn_gb300 import engine
+    eng = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"))
+    eng.serve_start(max_inflight=3, skin=1.0, flags=engine.BF16)
+    yield eng
+    eng.serve_stop()
+    eng.close()
+
+
+def test_alone_equals_in_the_mix(served):
+    target = W.make_structures("mixed512", seed=61, count=1, sizes=[333])[0]
+    e_alone, F_alone, _ = _wait(served, served.submit(target), target.natoms)
+    others = W.make_structures("mixed512", seed=62, count=40)
+    ids = []
+    for k, s in enumerate(others):
+        ids.append((served.submit(s), s))
+        if k == 20:
+            tid = served.submit(target)
+    res = [_wait(served, rid, s.natoms) for rid, s in ids]
+    e_mix, F_mix, _ = _wait(served, tid, target.natoms)
+    assert abs(e_mix - e_alone) / target.natoms <= E_TOL
+    assert np.abs(F_mix - F_alone).max() <= F_TOL
+    # and every result of the mix equals a direct evaluation of that structure
+    from atomnn_gb300 import engine
+    e_dir, F_dir, _ = served.compute([s for _, s in ids], engine.ENERGY | engine.FORCE | engine.BATCHED | engine.BF16)
+    for k, (e, F, lat) in enumerate(res):
+        assert abs(e - e_dir[k]) / ids[k][1].natoms <= E_TOL
+        assert np.abs(F - F_dir[k]).max() <= F_TOL
+        assert lat > 0
+
+
+def test_resident_md_steps_match_fresh_evaluation(served):
+    from atomnn_gb300 import engine
+    rng = np.random.default_rng(5)
+    base = W.make_structures("cell1728")[0]
+    posn = base.posn.copy()
+    for step in range(4):
+        s = W.Structure(posn=posn.copy(), species=base.species, cell=base.cell)
+        e, F, _ = _wait(served, served.submit(s, key=7), s.natoms)
+        e_ref, F_ref, _ = served.compute([s], engine.ENERGY | engine.FORCE | engine.BATCHED | engine.BF16)
+        assert abs(e - e_ref[0]) / s.natoms <= E_TOL
+        assert np.abs(F - F_ref[0]).max() <= F_TOL
+        posn += rng.uniform(-0.02, 0.02, size=posn.shape)  # MD-style step, well inside skin/2
+
+
+def test_oversized_request_refused(native_lib):
+    from atomnn_gb300 import engine
+    eng = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"))
+    eng.serve_start(max_inflight=2, max_batch_atoms=1000, skin=0.0)
+    s = W.make_structures("mixed512", seed=70, count=1, sizes=[1500])[0]
+    with pytest.raises(engine.NNPGPUError) as ei:
+        eng.submit(s)
+    assert ei.value.code == engine.ERR_OOM
+    small = W.make_structures("mixed512", seed=71, count=1, sizes=[200])[0]
+    e, F, _ = _wait(eng, eng.submit(small), small.natoms)
+    assert np.isfinite(e)
+    eng.serve_stop()
+    eng.close()
