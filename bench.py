@@ -307,7 +307,7 @@ def main():
 
     # batched FP32 (when the headline is BF16) and the plain path (one structure at a time)
     fp32_ms, _ = timed(batched, args.steps, 1) if bf16_ok else (ms, None)
-    plain_ms, _ = timed(E.ENERGY | E.FORCE, args.plain_steps, 1) if args.plain_steps > 0 else ([float("nan")], None)
+    plain_ms, _ = timed(E.ENERGY | E.FORCE, args.plain_steps, 1) if args.plain_steps > 0 else (None, None)
 
     # end to end through the host-buffer API (pinned staging, copies inside the timed region)
     h_energy = np.zeros(len(strucs))
@@ -401,13 +401,14 @@ def main():
             "gpu_launches": KERNELS_PER_BATCH * args.steps,
             "roofline": roof,
             "kernels": kernels,
-            "plain": {"value": total_atoms / (statistics.mean(plain_ms) / 1000), "unit": "atoms/s", "ms_per_step": statistics.mean(plain_ms),
-                      "desc": "one structure at a time (12 launches per structure), FP32 networks"},
+            "plain": None if plain_ms is None else {
+                "value": total_atoms / (statistics.mean(plain_ms) / 1000), "unit": "atoms/s", "ms_per_step": statistics.mean(plain_ms),
+                "desc": "one structure at a time (12 launches per structure), FP32 networks"},
             "batched_fp32": {"value": total_atoms / (statistics.mean(fp32_ms) / 1000), "unit": "atoms/s", "ms_per_step": statistics.mean(fp32_ms)},
             "accuracy_vs_fp64_oracle": acc,
             "serving": serve_out,
         }
-        if serve_out is not None and out["plain"]["value"] > 0:
+        if serve_out is not None and out["plain"] is not None:
             serve_out["saturated_vs_plain"] = serve_out["saturated"]["atoms_per_s"] / out["plain"]["value"]
         if cpu is not None:
             out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
