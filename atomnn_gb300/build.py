@@ -70,7 +70,36 @@ def build(verbose=False, ptxas_info=False, jobs=None):
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
         os.replace(LIB + ".tmp", LIB)
+    build_host()
     return LIB
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def build_host():
+    """The C++ host surface (libatomnn_gpu.so, include/atomnn_gpu.hpp) over libnnpgpu.so, and the
+    compute tool nnp_compute_gpu; both find libnnpgpu.so next to themselves."""
+    host = os.path.join(HERE, "host")
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    deps = [LIB, os.path.join(inc, "atomnn_gpu.hpp"), os.path.join(inc, "nnpgpu.h")]
+    shim_src = os.path.join(host, "atomnn_gpu.cpp")
+    shim = os.path.join(OUT, "libatomnn_gpu.so")
+    newest = max(os.path.getmtime(d) for d in deps + [shim_src])
+    if not os.path.exists(shim) or os.path.getmtime(shim) < newest:
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-shared", "-I" + inc, shim_src, "-o", shim + ".tmp", "-L" + OUT,
+              "-lnnpgpu", "-Wl,-rpath,$ORIGIN"])
+        os.replace(shim + ".tmp", shim)
+    tool_src = os.path.join(host, "nnp_compute_gpu.cpp")
+    tool = os.path.join(OUT, "nnp_compute_gpu")
+    if not os.path.exists(tool) or os.path.getmtime(tool) < max(newest, os.path.getmtime(shim), os.path.getmtime(tool_src)):
+        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + inc, tool_src, "-o", tool + ".tmp", "-L" + OUT, "-latomnn_gpu", "-lnnpgpu",
+              "-Wl,-rpath,$ORIGIN"])
+        os.replace(tool + ".tmp", tool)
+    return shim, tool
 
 
 if __name__ == "__main__":

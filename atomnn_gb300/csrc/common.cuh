@@ -70,10 +70,14 @@ struct NetsP {
 // Per-structure geometry of a batch.  mode: 0 non-periodic, 1 image shells (some shell > 0),
 // 2 single image (all shells 0: at most one image of each atom within the cutoff), 3 single
 // image with the candidate pairs taken from a resident skin list (skin_j/skin_code/skin_cnt,
-// local atom indices, skin_cap slots per atom) instead of all atoms of the structure.
+// local atom indices, skin_cap slots per atom) instead of all atoms of the structure, 4 single
+// image with the candidates taken from a cell list: nc[k] cells along fractional axis k, each
+// at least rc/reach wide, and the (2 reach + 1)^3 cells around the centre's cell searched;
+// the structure's cells occupy entries [cell0, cell0 + nc0*nc1*nc2] of the batch's cell arrays
+// (the last entry is the end sentinel).
 struct StrucMeta {
   int atom0, natoms, mode, nimg;
-  int img0, skin_cap, pad1, pad2;
+  int img0, skin_cap, cell0, reach;
   const int* skin_j;
   const int* skin_code;
   const int* skin_cnt;
@@ -83,11 +87,14 @@ struct StrucMeta {
   double shifts[18];     // +col0, -col0, +col1, -col1, +col2, -col2 (Cell::init, src/struc/cell.cpp:63-69)
   float Rf[9];
   float margin;          // FP32 filter margin on r^2
+  int nc[3];             // cell grid (mode 4)
+  int pad4;
 };
-// One lattice shift of the image box, in the reference's enumeration order.
+// One lattice shift of the image box, in the reference's enumeration order (vf = v in FP32).
 struct ImgEntry {
   double v[3];
   int n[3];
+  float vf[3];
   int pad;
 };
 
@@ -151,6 +158,15 @@ __host__ __device__ inline bool code_min(int c) { return (c >> 30) & 1; }
 __host__ __device__ inline int code_t(int c, int k) { return ((c >> (10 * k)) & 0x3ff) - 512; }
 
 #ifdef __CUDACC__
+// Round to nearest, ties to even (as rintf), for |x| < 2^22, with plain FP32 adds: adding
+// 1.5*2^23 leaves the rounded integer in the low mantissa bits.  k receives it as an int.
+__device__ __forceinline__ float round_even(float x, int& k) {
+  const float big = 12582912.0f;
+  const float t = __fadd_rn(x, big);
+  k = __float_as_int(t) - 0x4B400000;
+  return __fsub_rn(t, big);
+}
+
 // ---- cutoff functions (Basis::cut_func / cut_grad, src/nnp/basis.cpp:80-120), FP32
 __device__ __forceinline__ void cutoff_fg(int cut, float d, float rc, float pirc, float rci, float& f, float& g) {
   if (cut == CUT_COS) {

@@ -62,11 +62,11 @@ struct nnpgpu_ctx {
   nnpgpu::TuneCfg tune;
   // batch buffers
   nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, sfloor, nb_j, nb_r, nb_code, nb_cnt, nb_rev, orphans, G, dEdG, eatom, perm,
-      type_count, W, force, energy, status;
+      type_count, W, force, energy, status, cell_cnt, cell_start, cell_atoms, atom_cell;
   nnpgpu::HostBuf h_meta, h_in, h_out;  // pinned staging: geometry, inputs, outputs
   int buf_generation = 0;
   // captured launch sequences of the batched path, keyed by batch shape
-  typedef std::tuple<int, int, int, int, int, const void*, const void*, const void*, const void*> GraphKey;
+  typedef std::tuple<int, int, int, int, int, int, const void*, const void*, const void*, const void*> GraphKey;
   std::map<GraphKey, cudaGraphExec_t> graphs;
   std::map<GraphKey, int> shapes_seen;
   std::unique_ptr<nnpgpu::Serving> serving;

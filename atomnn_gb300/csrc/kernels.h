@@ -28,6 +28,12 @@ struct BatchDev {
   int* nb_code = nullptr;
   int* nb_cnt = nullptr;
   int* nb_rev = nullptr;
+  // cell lists of the structures in neighbour mode 4 (ncells entries, sentinels included)
+  int ncells = 0;
+  int* cell_cnt = nullptr;    // atoms per cell; zero between calls
+  int* cell_start = nullptr;  // first slot of each cell in cell_atoms (global atom positions)
+  int* cell_atoms = nullptr;  // [natoms] atoms ordered by cell
+  int* atom_cell = nullptr;   // [natoms] cell of each atom
   int* orphans = nullptr;
   int orphan_cap = 0;
   // descriptors and networks
@@ -52,6 +58,8 @@ struct TuneCfg {
 };
 
 void launch_neighbors(const BatchDev& B, cudaStream_t st);
+// dynamic shared memory of the neighbour kernel when some structure uses a cell list
+size_t neighbor_smem_bytes(int cap);
 void launch_reverse(const BatchDev& B, cudaStream_t st);
 // descriptors (NNP::symm) and chain rule (NNP::force) ; ne/nz select the template instance
 int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);

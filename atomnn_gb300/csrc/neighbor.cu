@@ -16,10 +16,11 @@
 
 namespace nnpgpu {
 
-// Wrapped fractional coordinates (FP32) and integer floors of R^-1 r, per atom.
+// Wrapped fractional coordinates (FP32) and integer floors of R^-1 r, per atom.  Atoms of a
+// cell-list structure (mode 4) are also binned: atom_cell[i] and the cell's atom count.
 __global__ void frac_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, const double* __restrict__ posn,
                             const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta, float4* __restrict__ sfrac,
-                            int4* __restrict__ sfloor, int* __restrict__ status) {
+                            int4* __restrict__ sfloor, int* __restrict__ atom_cell, int* __restrict__ cell_cnt, int* __restrict__ status) {
   const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a0 + natoms) return;
   const StrucMeta& S = meta[atom_struc[i]];
@@ -44,11 +45,79 @@ __global__ void frac_kernel(int a0, int natoms, int ntypes, const int* __restric
     }
     s = make_float4(sf[0], sf[1], sf[2], 0.f);
     fl = make_int4(fi[0], fi[1], fi[2], 0);
-  } else {
+  }  else {
     s = make_float4((float)p0, (float)p1, (float)p2, 0.f);
   }
   sfrac[i] = s;
   sfloor[i] = fl;
+  if (S.mode == 4) {
+    const int cx = min((int)(s.x * (float)S.nc[0]), S.nc[0] - 1);
+    const int cy = min((int)(s.y * (float)S.nc[1]), S.nc[1] - 1);
+    const int cz = min((int)(s.z * (float)S.nc[2]), S.nc[2] - 1);
+    const int c = S.cell0 + (cz * S.nc[1] + cy) * S.nc[0] + cx;
+    atom_cell[i] = c;
+    atomicAdd(&cell_cnt[c], 1);
+  }
+}
+
+// Exclusive scan of the cell counts of each cell-list structure (one CTA per structure):
+// cell_start[c] = the first position of cell c in cell_atoms; the entry after the last cell
+// is the structure's end.
+__global__ void __launch_bounds__(256) cell_scan_kernel(int s0, const StrucMeta* __restrict__ meta, const int* __restrict__ cell_cnt,
+                                                        int* __restrict__ cell_start) {
+  const StrucMeta& S = meta[s0 + blockIdx.x];
+  if (S.mode != 4) return;
+  __shared__ int wsum[8];
+  __shared__ int carry;
+  const int ncell = S.nc[0] * S.nc[1] * S.nc[2];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = S.atom0;
+  __syncthreads();
+  for (int base = 0; base < ncell; base += 1024) {
+    int v[4], t = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = base + 4 * threadIdx.x + q;
+      v[q] = c < ncell ? cell_cnt[S.cell0 + c] : 0;
+      t += v[q];
+    }
+    int incl = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int x = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += x;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    int before = carry;
+    for (int k = 0; k < w; ++k) before += wsum[k];
+    int run = before + incl - t;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = base + 4 * threadIdx.x + q;
+      if (c < ncell) cell_start[S.cell0 + c] = run;
+      run += v[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int k = 0; k < 8; ++k) carry += wsum[k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) cell_start[S.cell0 + ncell] = carry;
+}
+
+// Places each atom of a cell-list structure into its cell.  The count is taken back down to
+// zero on the way, so the counts are clean for the next call.  The order within a cell does
+// not matter: the neighbour kernel sorts every list by neighbour index.
+__global__ void cell_fill_kernel(int a0, int natoms, const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
+                                 const int* __restrict__ atom_cell, int* __restrict__ cell_cnt, const int* __restrict__ cell_start,
+                                 int* __restrict__ cell_atoms) {
+  const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a0 + natoms) return;
+  if (meta[atom_struc[i]].mode != 4) return;
+  const int c = atom_cell[i];
+  const int pos = cell_start[c] + atomicSub(&cell_cnt[c], 1) - 1;
+  cell_atoms[pos] = i;
 }
 
 __device__ __forceinline__ void emit(int slot, int cap, int j, float rx, float ry, float rz, float dr, int code,
@@ -78,8 +147,8 @@ __device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& 
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     // mod(f,-0.5,0.5) rounds half-integers up: D = floor(f + 0.5)
-    const float t = dl[k] + 0.5f;
-    const float fk = floorf(t);
+    const float t = dl[k] + 0.5f;  // in (-0.5, 1.5): the floor is one of -1, 0, 1
+    const float fk = (t >= 1.0f) ? 1.0f : ((t >= 0.0f) ? 0.0f : -1.0f);
     const float fr = t - fk;
     if (fr < eps || fr > 1.0f - eps) ok = false;
     d[k] = dl[k] - fk;
@@ -106,11 +175,51 @@ __device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& 
   return ok;
 }
 
+// Single-image decision (modes 2 and 4) for centre i and candidate j: the Cell::diff image of
+// j is kept when |diff|^2 <= rc^2.  FP32 from the wrapped fractional coordinates, with the FP64
+// replay of Cell::diff when |diff|^2 lies within the margin of rc^2.
+__device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& si, const int4& fi, int j, const float4* __restrict__ sfrac,
+                                             const int4* __restrict__ sfloor, const double* __restrict__ posn, double pi0, double pi1,
+                                             double pi2, double rc2, float rc2f, float m, float& r0, float& r1, float& r2, float& dr,
+                                             int D[3]) {
+  const float4 sj = sfrac[j];
+  const float dl0 = si.x - sj.x, dl1 = si.y - sj.y, dl2 = si.z - sj.z;
+  int k0, k1, k2;
+  const float q0 = round_even(dl0, k0), q1 = round_even(dl1, k1), q2 = round_even(dl2, k2);
+  rf_mul(S, dl0 - q0, dl1 - q1, dl2 - q2, r0, r1, r2);
+  const float d2f = r0 * r0 + r1 * r1 + r2 * r2;
+  if (d2f > rc2f + m) return false;
+  const int4 fj = sfloor[j];
+  D[0] = k0 + fi.x - fj.x;
+  D[1] = k1 + fi.y - fj.y;
+  D[2] = k2 + fi.z - fj.z;
+  if (d2f < rc2f - m) {
+    dr = sqrtf(d2f);
+    return true;
+  }
+  double o0, o1, o2;
+  cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], o0, o1, o2, D);
+  const double d2 = sqn3(o0, o1, o2);
+  r0 = (float)o0;
+  r1 = (float)o1;
+  r2 = (float)o2;
+  dr = (float)sqrt(d2);
+  return d2 <= rc2;
+}
+
+// Per-warp shared memory of the cell-list path: staged slots (cap), candidate ranges and the
+// bit mask used to rank the staged neighbours by index.
+constexpr int NB_RANGES = 128;  // >= 2 (2*3+1)^2 rows of the widest stencil (reach 3)
+constexpr int NB_MASK_WORDS = 128;  // structures up to 4096 atoms rank through the bit mask
+__host__ __device__ inline size_t nb_warp_smem(int cap) { return (size_t)cap * 24 + 4 * (2 * NB_RANGES + 2 * NB_MASK_WORDS); }
+size_t neighbor_smem_bytes(int cap) { return 4 * nb_warp_smem(cap); }
+
 __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int cap, double rc, const double* __restrict__ posn,
                                                        const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
                                                        const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
-                                                       const ImgEntry* __restrict__ imgs, int* __restrict__ nb_j,
-                                                       float4* __restrict__ nb_r, int* __restrict__ nb_code,
+                                                       const ImgEntry* __restrict__ imgs, const int* __restrict__ atom_cell,
+                                                       const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
+                                                       int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
                                                        int* __restrict__ nb_cnt, int* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -136,33 +245,150 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       bool keep = false;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       int D[3] = {0, 0, 0};
-      if (jl < nj && j != i) {
-        const float4 sj = sfrac[j];
-        const float dl0 = si.x - sj.x, dl1 = si.y - sj.y, dl2 = si.z - sj.z;
-        const float k0 = rintf(dl0), k1 = rintf(dl1), k2 = rintf(dl2);
-        rf_mul(S, dl0 - k0, dl1 - k1, dl2 - k2, r0, r1, r2);
-        const float d2f = r0 * r0 + r1 * r1 + r2 * r2;
-        if (d2f <= rc2f + m) {
-          const int4 fj = sfloor[j];
-          D[0] = (int)k0 + fi.x - fj.x;
-          D[1] = (int)k1 + fi.y - fj.y;
-          D[2] = (int)k2 + fi.z - fj.z;
-          if (d2f < rc2f - m) {
-            keep = true;
-            dr = sqrtf(d2f);
-          } else {
-            double o0, o1, o2;
-            cell_diff(S, pi0, pi1, pi2, posn[3 * j], posn[3 * j + 1], posn[3 * j + 2], o0, o1, o2, D);
-            const double d2 = sqn3(o0, o1, o2);
-            keep = d2 <= rc2;
-            r0 = (float)o0; r1 = (float)o1; r2 = (float)o2;
-            dr = (float)sqrt(d2);
-          }
-        }
-      }
+      if (jl < nj && j != i) keep = single_image(S, si, fi, j, sfrac, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc);
       count += __popc(mk);
+    }
+  } else if (S.mode == 4) {
+    // cell list: the candidates are the atoms of the (2 reach + 1)^3 cells around the centre's
+    // cell, visited as contiguous x-runs of cells (two runs where the stencil wraps); accepted
+    // neighbours are staged in shared memory and written out in increasing index order.
+    extern __shared__ __align__(16) unsigned char nb_smem[];
+    unsigned char* wbase = nb_smem + (size_t)(threadIdx.x >> 5) * nb_warp_smem(cap);
+    float4* st_r = (float4*)wbase;
+    int* st_j = (int*)(st_r + cap);
+    int* st_c = st_j + cap;
+    int* rb = st_c + cap;           // range begin (position in cell_atoms)
+    int* rp = rb + NB_RANGES;       // range prefix (candidate numbering)
+    unsigned* msk = (unsigned*)(rp + NB_RANGES);
+    int* wpre = (int*)(msk + NB_MASK_WORDS);
+    const int k = S.reach, nx = S.nc[0], ny = S.nc[1], nz = S.nc[2];
+    const int side = 2 * k + 1, nrow = side * side;
+    const int ci = atom_cell[i] - S.cell0;
+    const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
+    // ranges 2q, 2q+1 of row q: start[] is monotone, so a run of cells is one slice of cell_atoms
+    int len[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const int r = 4 * lane + t;
+      const int q = r >> 1;
+      int begin = 0, n = 0;
+      if (q < nrow) {
+        int y = cy + (q % side) - k, z = cz + (q / side) - k;
+        y += (y < 0) ? ny : ((y >= ny) ? -ny : 0);
+        z += (z < 0) ? nz : ((z >= nz) ? -nz : 0);
+        const int row = S.cell0 + (z * ny + y) * nx;
+        const int xlo = cx - k, xhi = cx + k;
+        int a, b;  // cells [a, b] of this part, b < a means empty
+        if (xlo < 0) {
+          a = (r & 1) ? 0 : xlo + nx;
+          b = (r & 1) ? xhi : nx - 1;
+        } else if (xhi >= nx) {
+          a = (r & 1) ? 0 : xlo;
+          b = (r & 1) ? xhi - nx : nx - 1;
+        } else {
+          a = xlo;
+          b = (r & 1) ? xlo - 1 : xhi;
+        }
+        if (b >= a) {
+          begin = cell_start[row + a];
+          n = cell_start[row + b + 1] - begin;
+        }
+      }
+      len[t] = n;
+      if (r < NB_RANGES) rb[r] = begin;
+    }
+    const int lsum = len[0] + len[1] + len[2] + len[3];
+    int incl = lsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int run = incl - lsum;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      rp[4 * lane + t] = run;
+      run += len[t];
+    }
+    const int nr = 2 * nrow;
+    __syncwarp();
+    const float4 si = sfrac[i];
+    const int4 fi = sfloor[i];
+    for (int c = 0; c < total; c += 32) {
+      const int qd = c + lane;
+      bool keep = false;
+      float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
+      int D[3] = {0, 0, 0};
+      int j = -1;
+      if (qd < total) {
+        int lo = 0, hi = nr - 1;  // last range with prefix <= qd
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (rp[mid] <= qd) lo = mid;
+          else hi = mid - 1;
+        }
+        j = cell_atoms[rb[lo] + qd - rp[lo]];
+        if (j != i) keep = single_image(S, si, fi, j, sfrac, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
+      }
+      const unsigned mk = __ballot_sync(0xffffffffu, keep);
+      const int slot = count + __popc(mk & lt);
+      if (keep && slot < cap) {
+        st_j[slot] = j;
+        st_r[slot] = make_float4(r0, r1, r2, dr);
+        st_c[slot] = pack_code(D[0], D[1], D[2], true);
+      }
+      count += __popc(mk);
+    }
+    __syncwarp();
+    const int n = min(count, cap);
+    if (nj <= 32 * NB_MASK_WORDS) {
+      // rank = number of staged neighbours with a smaller index, read off a bit mask
+#pragma unroll
+      for (int t = 0; t < NB_MASK_WORDS / 32; ++t) msk[lane + 32 * t] = 0u;
+      __syncwarp();
+      for (int e = lane; e < n; e += 32) {
+        const int jl = st_j[e] - j0;
+        atomicOr(&msk[jl >> 5], 1u << (jl & 31));
+      }
+      __syncwarp();
+      int wc[NB_MASK_WORDS / 32], ws = 0;
+#pragma unroll
+      for (int t = 0; t < NB_MASK_WORDS / 32; ++t) {
+        wc[t] = __popc(msk[4 * lane + t]);
+        ws += wc[t];
+      }
+      int winc = ws;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, winc, o);
+        if (lane >= o) winc += v;
+      }
+      int wrun = winc - ws;
+#pragma unroll
+      for (int t = 0; t < NB_MASK_WORDS / 32; ++t) {
+        wpre[4 * lane + t] = wrun;
+        wrun += wc[t];
+      }
+      __syncwarp();
+      for (int e = lane; e < n; e += 32) {
+        const int jg = st_j[e], jl = jg - j0;
+        const int rank = wpre[jl >> 5] + __popc(msk[jl >> 5] & ((1u << (jl & 31)) - 1u));
+        oj[rank] = jg;
+        orr[rank] = st_r[e];
+        oc[rank] = st_c[e];
+      }
+    } else {
+      for (int e = lane; e < n; e += 32) {
+        const int jg = st_j[e];
+        int rank = 0;
+        for (int f = 0; f < n; ++f) rank += (st_j[f] < jg) ? 1 : 0;
+        oj[rank] = jg;
+        orr[rank] = st_r[e];
+        oc[rank] = st_c[e];
+      }
     }
   } else if (S.mode == 3) {
     // resident skin list (built with a larger cutoff at some earlier positions): the candidates
@@ -231,7 +457,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
         if (ok) {
           float mn = 3.4e38f, second = 3.4e38f;
           for (int n = 0; n < nimg; ++n) {
-            const float t0 = o0 - (float)im[n].v[0], t1 = o1 - (float)im[n].v[1], t2 = o2 - (float)im[n].v[2];
+            const float t0 = o0 - im[n].vf[0], t1 = o1 - im[n].vf[1], t2 = o2 - im[n].vf[2];
             const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
             if (fabsf(d2 - rc2f) <= m) { ok = false; break; }
             const bool keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
@@ -286,7 +512,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
             t0 = (float)e0; t1 = (float)e1; t2 = (float)e2;
             dr = keep ? (float)sqrt(d2) : 0.f;
           } else {
-            t0 = o0 - (float)im[n].v[0]; t1 = o1 - (float)im[n].v[1]; t2 = o2 - (float)im[n].v[2];
+            t0 = o0 - im[n].vf[0]; t1 = o1 - im[n].vf[1]; t2 = o2 - im[n].vf[2];
             const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
             keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
             dr = sqrtf(d2);
@@ -371,10 +597,19 @@ __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int ca
 void launch_neighbors(const BatchDev& B, cudaStream_t st) {
   if (B.natoms == 0) return;
   frac_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.ntypes, B.type, B.posn, B.atom_struc, B.meta, B.sfrac,
-                                                      B.sfloor, B.status);
+                                                      B.sfloor, B.atom_cell, B.cell_cnt, B.status);
+  size_t smem = 0;
+  if (B.ncells > 0) {
+    cell_scan_kernel<<<B.nstruc, 256, 0, st>>>(B.s0, B.meta, B.cell_cnt, B.cell_start);
+    cell_fill_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.atom_struc, B.meta, B.atom_cell, B.cell_cnt, B.cell_start,
+                                                             B.cell_atoms);
+    smem = neighbor_smem_bytes(B.cap);
+    static bool attr = false;  // skin lists may ask for up to 1024 slots per atom (106 KB)
+    if (!attr) attr = cudaFuncSetAttribute(neighbor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  }
   const int blocks = (B.natoms + 3) / 4;
-  neighbor_kernel<<<blocks, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
-                                          B.nb_j, B.nb_r, B.nb_code, B.nb_cnt, B.status);
+  neighbor_kernel<<<blocks, 128, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
+                                             B.atom_cell, B.cell_start, B.cell_atoms, B.nb_j, B.nb_r, B.nb_code, B.nb_cnt, B.status);
 }
 
 void launch_reverse(const BatchDev& B, cudaStream_t st) {

@@ -61,6 +61,40 @@ bool ensure_host(nnpgpu_ctx* c, HostBuf& b, size_t bytes) {
 
 static double nrm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 
+// Cell grid of a single-image structure (mode 2 -> 4).  Along fractional axis k the cell
+// count is the largest nc with width h_k / nc >= rc / reach + slack (h_k = 1/|row k of R^-1|,
+// the distance between the cell's faces), so that any atom within rc of a centre lies within
+// reach cells of the centre's cell; nc >= 2 reach + 1 keeps the stencil's cells distinct.  The
+// reach with the fewest candidates wins; brute force stays when cells would not pay.
+static void choose_cells(StrucMeta& m, int natoms, double rc) {
+  double h[3];
+  for (int k = 0; k < 3; ++k) {
+    const double a = m.RInv[k], b = m.RInv[3 + k], c = m.RInv[6 + k];
+    h[k] = 1.0 / std::sqrt(a * a + b * b + c * c);
+  }
+  double best = 0.5;  // candidate fraction that the cell path must beat
+  for (int reach = 1; reach <= 3; ++reach) {
+    const double w = rc / reach + 1e-4 * rc + 1e-3;
+    int nc[3];
+    bool ok = true;
+    double cells = 1;
+    for (int k = 0; k < 3; ++k) {
+      const double q = std::floor(h[k] / w);
+      nc[k] = q > 1024 ? 1024 : (int)q;
+      ok = ok && nc[k] >= 2 * reach + 1;
+      cells *= nc[k];
+    }
+    if (!ok || cells > 4.0 * natoms + 64) continue;
+    const double frac = std::pow(2.0 * reach + 1, 3) / cells;
+    if (frac < best) {
+      best = frac;
+      m.mode = 4;
+      m.reach = reach;
+      for (int k = 0; k < 3; ++k) m.nc[k] = nc[k];
+    }
+  }
+}
+
 void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& m, std::vector<ImgEntry>& imgs) {
   std::memset(&m, 0, sizeof(m));
   m.atom0 = atom0;
@@ -126,6 +160,7 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
   m.margin = (float)(2.0 * rc * (Lsum * 1e-6 + 1e-5) + 1e-4 * rc * rc);
   if (shell[0] == 0 && shell[1] == 0 && shell[2] == 0) {
     m.mode = 2;
+    choose_cells(m, natoms, rc);
     return;
   }
   m.mode = 1;
@@ -135,7 +170,10 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
       for (int k = -shell[2]; k <= shell[2]; ++k) {
         ImgEntry e;
         std::memset(&e, 0, sizeof(e));
-        for (int x = 0; x < 3; ++x) e.v[x] = i * R0[x] + j * R1[x] + k * R2[x];
+        for (int x = 0; x < 3; ++x) {
+          e.v[x] = i * R0[x] + j * R1[x] + k * R2[x];
+          e.vf[x] = (float)e.v[x];
+        }
         e.n[perm[0]] = i;
         e.n[perm[1]] = j;
         e.n[perm[2]] = k;
@@ -158,7 +196,7 @@ static int estimate_cap(const nnpgpu_ctx* c, int nstruc, const int* natoms, cons
   }
   int cap = (int)std::ceil(best / 32.0) * 32;
   if (c->cap_hint > 0) cap = (c->cap_hint + 31) / 32 * 32;  // explicit or learned capacity
-  return std::min(cap, 256);
+  return std::min(cap, 1024);
 }
 
 int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
@@ -210,7 +248,7 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
 namespace {
 
 struct Uploaded {
-  int natoms = 0, nstruc = 0, cap = 0;
+  int natoms = 0, nstruc = 0, cap = 0, ncells = 0;
   std::vector<StrucMeta> metas;
   std::vector<int> offsets;
 };
@@ -231,7 +269,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
   try {
     for (int s = 0; s < nstruc; ++s) {
       make_meta(cell + 9 * s, U.offsets[s], natoms[s], c->pot.rc, U.metas[s], imgs);
-      if (skins && skins[s].cnt && U.metas[s].mode == 2) {
+      if (skins && skins[s].cnt && (U.metas[s].mode == 2 || U.metas[s].mode == 4)) {
         U.metas[s].mode = 3;
         U.metas[s].skin_j = skins[s].j;
         U.metas[s].skin_code = skins[s].code;
@@ -242,6 +280,12 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
   } catch (PotError& e) {
     return set_error(c, e.code, e.what());
   }
+  U.ncells = 0;
+  for (int s = 0; s < nstruc; ++s)
+    if (U.metas[s].mode == 4) {
+      U.metas[s].cell0 = U.ncells;
+      U.ncells += U.metas[s].nc[0] * U.metas[s].nc[1] * U.metas[s].nc[2] + 1;
+    }
   if (imgs.empty()) imgs.resize(1);
   U.cap = cap;
   const size_t N = std::max(U.natoms, 1);
@@ -257,6 +301,13 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
        ensure(c, c->type_count, sizeof(int) * (3 * NT_MAX + 3)) && ensure(c, c->W, sizeof(float4) * NC) &&
        ensure(c, c->force, sizeof(double) * 3 * N) && ensure(c, c->energy, sizeof(double) * std::max(nstruc, 1)) &&
        ensure(c, c->status, sizeof(int) * ST_WORDS);
+  if (ok && U.ncells > 0) {
+    // cell counts must start at zero: fresh memory is cleared, later calls leave them at zero
+    const size_t before = c->cell_cnt.bytes;  // a grown buffer is a new allocation
+    ok = ensure(c, c->cell_cnt, sizeof(int) * U.ncells) && ensure(c, c->cell_start, sizeof(int) * U.ncells) &&
+         ensure(c, c->cell_atoms, sizeof(int) * N) && ensure(c, c->atom_cell, sizeof(int) * N);
+    if (ok && c->cell_cnt.bytes != before) cudaMemsetAsync(c->cell_cnt.p, 0, c->cell_cnt.bytes, st);
+  }
   if (!ok) return set_error(c, NNPGPU_ERR_OOM, "device allocation failed or HBM budget exceeded");
   // atom -> structure map and metadata
   std::vector<int> as(N, 0);
@@ -295,6 +346,13 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.nb_code = (int*)c->nb_code.p;
   B.nb_cnt = (int*)c->nb_cnt.p;
   B.nb_rev = (int*)c->nb_rev.p;
+  B.ncells = U.ncells;
+  if (U.ncells > 0) {
+    B.cell_cnt = (int*)c->cell_cnt.p;
+    B.cell_start = (int*)c->cell_start.p;
+    B.cell_atoms = (int*)c->cell_atoms.p;
+    B.atom_cell = (int*)c->atom_cell.p;
+  }
   B.orphans = (int*)c->orphans.p;
   B.orphan_cap = std::max(U.natoms, 1);
   B.G = (float*)c->G.p;
@@ -313,7 +371,8 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
 // Enqueues the pipeline for the whole batch (batched) or one structure at a time (plain).
 int enqueue(nnpgpu_ctx* c, const Uploaded& U, const BatchDev& Ball, int flags, cudaStream_t st) {
   if (flags & NNPGPU_BATCHED) {
-    const nnpgpu_ctx::GraphKey key(U.natoms, U.nstruc, U.cap, flags, c->buf_generation, Ball.posn, Ball.type, Ball.energy, Ball.force);
+    const nnpgpu_ctx::GraphKey key(U.natoms, U.nstruc, U.cap, flags, c->buf_generation, U.ncells, Ball.posn, Ball.type, Ball.energy,
+                                   Ball.force);
     auto it = c->graphs.find(key);
     if (it != c->graphs.end()) {
       const cudaError_t e = cudaGraphLaunch(it->second, st);
@@ -486,7 +545,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
-                    &c->status};
+                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);
@@ -556,7 +615,7 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
   if (!device_io)
     for (int a = 0; a < total; ++a)
       if (species[a] < 0 || species[a] >= c->pot.ntypes) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
-  int cap = estimate_cap(c, nstruc, natoms, cell);
+  int cap = std::min(256, estimate_cap(c, nstruc, natoms, cell));  // the descriptor kernels take at most 256 slots
   for (int attempt = 0; attempt < 4; ++attempt) {
     Uploaded U;
     int rc = prepare(c, nstruc, natoms, cell, cap, U, st, skins);
@@ -668,20 +727,29 @@ extern "C" int nnpgpu_compute_device(nnpgpu_ctx* c, int nstruc, const int* natom
   return compute_impl(c, nstruc, natoms, d_posn, d_species, cell, flags, d_energy, d_force, d_symm, true, (cudaStream_t)stream);
 }
 
-extern "C" int nnpgpu_neighbors(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, int cap, int* count, int* index,
-                                float* r, unsigned char* mn, int* shift) {
+// Neighbour list of one structure at cutoff rc (the potential's when rc <= 0), at most
+// max_slots device slots per atom.
+static int neighbors_impl(nnpgpu_ctx* c, double rc_req, int max_slots, int natoms, const double* posn, const double* cell, int cap,
+                          int* count, int* index, float* r, unsigned char* mn, int* shift) {
   if (!c || natoms < 0 || cap <= 0 || (natoms > 0 && (!posn || !count))) return set_error(c, NNPGPU_ERR_INVALID, "invalid arguments");
+  if (!(rc_req <= 0) && !(rc_req < 1e6)) return set_error(c, NNPGPU_ERR_INVALID, "invalid cutoff");
   if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;
   const double zero[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   const double* cl = cell ? cell : zero;
-  const int dcap = std::min(256, std::max(cap, estimate_cap(c, 1, &natoms, cl)));
+  // the geometry set-up (shells, cell grid) and the capacity estimate follow the requested cutoff
+  const double saved = c->pot.rc;
+  if (rc_req > 0) c->pot.rc = rc_req;
+  const int est = estimate_cap(c, 1, &natoms, cl);
+  const int dcap = std::min(max_slots, std::max(cap, est));
   Uploaded U;
   int rc = prepare(c, 1, &natoms, cl, (dcap + 31) / 32 * 32, U, st);
+  c->pot.rc = saved;
   if (rc != NNPGPU_OK) return rc;
   cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, st);
   BatchDev B = batch_view(c, U, (const double*)c->posn.p, nullptr, (double*)c->energy.p, (double*)c->force.p);
+  if (rc_req > 0) B.rc = rc_req;
   launch_neighbors(B, st);
   std::vector<int> hj((size_t)natoms * U.cap), hc((size_t)natoms * U.cap), hn(natoms);
   std::vector<float4> hr((size_t)natoms * U.cap);
@@ -707,6 +775,18 @@ extern "C" int nnpgpu_neighbors(nnpgpu_ctx* c, int natoms, const double* posn, c
       if (shift) for (int x = 0; x < 3; ++x) shift[3 * dst + x] = code_t(hc[src], x);
     }
   }
-  if (status == NNPGPU_OK && hstat[ST_MAXCOUNT] > U.cap) status = set_error(c, NNPGPU_ERR_CAPACITY, "neighbour list longer than 256");
+  if (status == NNPGPU_OK && hstat[ST_MAXCOUNT] > U.cap)
+    status = set_error(c, NNPGPU_ERR_CAPACITY, "neighbour list longer than " + std::to_string(max_slots));
   return status;
+}
+
+extern "C" int nnpgpu_neighbors(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, int cap, int* count, int* index,
+                                float* r, unsigned char* mn, int* shift) {
+  return neighbors_impl(c, 0.0, 256, natoms, posn, cell, cap, count, index, r, mn, shift);
+}
+
+extern "C" int nnpgpu_neighbors_rc(nnpgpu_ctx* c, double rc, int natoms, const double* posn, const double* cell, int cap, int* count,
+                                   int* index, float* r, unsigned char* mn, int* shift) {
+  if (!(rc > 0)) return set_error(c, NNPGPU_ERR_INVALID, "cutoff must be positive");
+  return neighbors_impl(c, rc, 1024, natoms, posn, cell, cap, count, index, r, mn, shift);
 }

@@ -151,7 +151,10 @@ int fixed_meta(const double* cell, int natoms, double rc, StrucMeta& m, ImgEntry
       for (int k = -shell[2]; k <= shell[2]; ++k) {
         ImgEntry& e = imgs[nimg++];
         std::memset(&e, 0, sizeof(e));
-        for (int x = 0; x < 3; ++x) e.v[x] = i * R0[x] + j * R1[x] + k * R2[x];
+        for (int x = 0; x < 3; ++x) {
+          e.v[x] = i * R0[x] + j * R1[x] + k * R2[x];
+          e.vf[x] = (float)e.v[x];
+        }
         e.n[perm[0]] = i;
         e.n[perm[1]] = j;
         e.n[perm[2]] = k;

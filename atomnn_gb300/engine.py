@@ -16,7 +16,7 @@ ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 
 # every symbol the header declares
 EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
-           "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_serve_start", "nnpgpu_submit",
+           "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
            "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc"]
 
@@ -61,6 +61,7 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_compute.argtypes = [vp, ip, vp, vp, vp, vp, ip, vp, vp, vp]
     L.nnpgpu_compute_device.argtypes = [vp, ip, vp, vp, vp, vp, ip, vp, vp, vp, vp]
     L.nnpgpu_neighbors.argtypes = [vp, ip, vp, vp, ip, vp, vp, vp, vp, vp]
+    L.nnpgpu_neighbors_rc.argtypes = [vp, dp, ip, vp, vp, ip, vp, vp, vp, vp, vp]
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
     L.nnpgpu_submit.argtypes = [vp, ip, vp, vp, vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
     L.nnpgpu_poll.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.POINTER(ctypes.c_double)]
@@ -196,8 +197,9 @@ class Engine:
             out[self.lib.nnpgpu_profile_stage_name(k).decode()] = (ms.value, n.value)
         return out
 
-    def neighbors(self, posn, cell, cap=256):
-        """Neighbour list of one structure built on the GPU (reference list order)."""
+    def neighbors(self, posn, cell, cap=256, rc=None):
+        """Neighbour list of one structure built on the GPU (reference list order), at the
+        potential's cutoff or at ``rc``."""
         posn = np.ascontiguousarray(posn, dtype=np.float64)
         n = posn.shape[0]
         count = np.zeros(n, dtype=np.int32)
@@ -205,7 +207,11 @@ class Engine:
         r = np.zeros((n, cap, 4), dtype=np.float32)
         mn = np.zeros((n, cap), dtype=np.uint8)
         sh = np.zeros((n, cap, 3), dtype=np.int32)
-        self._check(self.lib.nnpgpu_neighbors(self._ctx, n, _p(posn), _p(_cell_colmajor(cell)), cap, _p(count), _p(index), _p(r),
-                                              _p(mn), _p(sh)))
+        if rc is None:
+            self._check(self.lib.nnpgpu_neighbors(self._ctx, n, _p(posn), _p(_cell_colmajor(cell)), cap, _p(count), _p(index), _p(r),
+                                                  _p(mn), _p(sh)))
+        else:
+            self._check(self.lib.nnpgpu_neighbors_rc(self._ctx, float(rc), n, _p(posn), _p(_cell_colmajor(cell)), cap, _p(count),
+                                                     _p(index), _p(r), _p(mn), _p(sh)))
         return [dict(index=index[i, :count[i]].copy(), r=r[i, :count[i], :3].astype(np.float64), dr=r[i, :count[i], 3].astype(np.float64),
                      min=mn[i, :count[i]].astype(bool), shift=sh[i, :count[i]].copy()) for i in range(n)]

@@ -1,0 +1,421 @@
+// atomnn_gpu.cpp - the C++ host surface (include/atomnn_gpu.hpp) over the C ABI (nnpgpu.h).
+#include "../../include/atomnn_gpu.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+
+namespace atomnn_gpu {
+
+namespace {
+
+// Status code -> the exception the reference throws for the same failure.
+[[noreturn]] void fail(nnpgpu_ctx* ctx, int code, const char* where) {
+  const std::string msg = std::string(where) + ": " + (ctx ? nnpgpu_last_error(ctx) : "no context");
+  if (code == NNPGPU_ERR_INVALID) throw std::invalid_argument(msg);
+  throw std::runtime_error(msg);
+}
+
+void check(nnpgpu_ctx* ctx, int code, const char* where) {
+  if (code != NNPGPU_OK) fail(ctx, code, where);
+}
+
+// The context of the most recently read potential, for NeighborList::build(struc, rc).
+std::mutex g_last_mu;
+std::weak_ptr<nnpgpu_ctx> g_last;
+
+std::string upper(std::string s) {
+  for (char& ch : s) ch = (char)std::toupper((unsigned char)ch);
+  return s;
+}
+
+// whitespace tokens of a line after removing a '#' comment
+std::vector<std::string> tokens(const std::string& line) {
+  std::string s = line.substr(0, line.find('#'));
+  std::istringstream in(s);
+  std::vector<std::string> out;
+  std::string t;
+  while (in >> t) out.push_back(t);
+  return out;
+}
+
+struct Flat {
+  std::vector<int> natoms, species;
+  std::vector<double> posn, cell;
+};
+
+void flatten(const NNP& nnp, const Structure* const* strucs, int n, Flat& f) {
+  f.natoms.resize(n);
+  f.cell.resize(9 * (size_t)n);
+  size_t tot = 0;
+  for (int s = 0; s < n; ++s) tot += (size_t)strucs[s]->nAtoms();
+  f.posn.resize(3 * tot);
+  f.species.resize(tot);
+  size_t a = 0;
+  for (int s = 0; s < n; ++s) {
+    const Structure& st = *strucs[s];
+    f.natoms[s] = st.nAtoms();
+    for (int k = 0; k < 9; ++k) f.cell[9 * (size_t)s + k] = st.R()[k];
+    for (int i = 0; i < st.nAtoms(); ++i, ++a) {
+      for (int x = 0; x < 3; ++x) f.posn[3 * a + x] = st.posn(i)[x];
+      const int t = st.type(i);
+      if (t < 0 || t >= nnp.ntypes())
+        throw std::invalid_argument("atom " + std::to_string(i) + " has type " + std::to_string(t) +
+                                    ", not a type of the potential (set struc.type(i) = nnp.index(name))");
+      f.species[a] = t;
+    }
+  }
+}
+
+int max_input(const NNP& nnp) {
+  int m = 0;
+  for (int t = 0; t < nnp.ntypes(); ++t) m = std::max(m, nnp.nInput(t));
+  return m;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------ Structure
+void Structure::resize(int nAtoms) {
+  if (nAtoms < 0) throw std::invalid_argument("Structure::resize: negative atom count");
+  nAtoms_ = nAtoms;
+  name_.resize(nAtoms);
+  type_.resize(nAtoms, -1);
+  index_.resize(nAtoms);
+  for (int i = 0; i < nAtoms; ++i) index_[i] = i;
+  posn_.resize(nAtoms);
+  force_.resize(nAtoms);
+  symm_.resize(nAtoms);
+}
+
+void Structure::clear() {
+  *this = Structure();
+}
+
+void Structure::init(const double lv[9]) {
+  for (int k = 0; k < 9; ++k) R_[k] = lv[k];
+}
+
+bool Structure::periodic() const {
+  for (double v : R_)
+    if (v != 0.0) return true;
+  return false;
+}
+
+// ------------------------------------------------------------------------------ NNP
+int NNP::ntypes() const { return ctx_ ? nnpgpu_ntypes(ctx_.get()) : 0; }
+int NNP::index(const char* name) const { return ctx_ ? nnpgpu_type_index(ctx_.get(), name) : -1; }
+double NNP::rc() const { return ctx_ ? nnpgpu_cutoff(ctx_.get()) : 0.0; }
+int NNP::nInput(int type) const { return ctx_ ? nnpgpu_ninput(ctx_.get(), type) : -1; }
+
+void NNP::read(const char* file, NNP& nnp, const nnpgpu_opts* opts) {
+  if (!file) throw std::invalid_argument("NNP::read: no file");
+  nnpgpu_ctx* c = nullptr;
+  const int code = nnpgpu_create(file, opts, &c);
+  std::shared_ptr<nnpgpu_ctx> holder(c, [](nnpgpu_ctx* p) { nnpgpu_destroy(p); });
+  if (code != NNPGPU_OK) fail(c, code, "NNP::read");
+  nnp.ctx_ = holder;
+  nnp.file_ = file;
+  nnp.cached_ = false;
+  std::lock_guard<std::mutex> l(g_last_mu);
+  g_last = holder;
+}
+
+uint64_t NNP::fingerprint(const Structure& struc) {
+  // FNV-1a over atom count, lattice, types and positions
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](const void* p, size_t n) {
+    const unsigned char* b = (const unsigned char*)p;
+    for (size_t k = 0; k < n; ++k) h = (h ^ b[k]) * 1099511628211ull;
+  };
+  const int n = struc.nAtoms();
+  mix(&n, sizeof(n));
+  mix(struc.R().data(), sizeof(double) * 9);
+  if (n > 0) {
+    mix(struc.type().data(), sizeof(int) * n);
+    mix(struc.posn().data(), sizeof(Vec3d) * n);
+  }
+  return h;
+}
+
+void NNP::init(const NNP& nnp, Structure& struc) {
+  for (int i = 0; i < struc.nAtoms(); ++i) {
+    const int t = struc.type(i);
+    if (t < 0 || t >= nnp.ntypes()) throw std::invalid_argument("NNP::init: atom type not in the potential");
+    struc.symm(i).assign(nnp.nInput(t), 0.0);
+  }
+}
+
+void NNP::symm(NNP& nnp, Structure& struc, const NeighborList&) {
+  if (!nnp.ctx_) throw std::runtime_error("NNP::symm: no potential read");
+  const Structure* p = &struc;
+  Flat f;
+  flatten(nnp, &p, 1, f);
+  const int stride = max_input(nnp);
+  std::vector<float> G((size_t)std::max(struc.nAtoms(), 1) * stride);
+  double e = 0.0;
+  const int flags = NNPGPU_SYMM | NNPGPU_ENERGY | (nnp.bf16_ ? NNPGPU_BF16 : 0);
+  check(nnp.ctx(), nnpgpu_compute(nnp.ctx(), 1, f.natoms.data(), f.posn.data(), f.species.data(), f.cell.data(), flags, &e, nullptr, G.data()),
+        "NNP::symm");
+  for (int i = 0; i < struc.nAtoms(); ++i) {
+    const int nin = nnp.nInput(struc.type(i));
+    struc.symm(i).resize(nin);
+    for (int k = 0; k < nin; ++k) struc.symm(i)[k] = G[(size_t)i * stride + k];
+  }
+  nnp.cached_key_ = fingerprint(struc);
+  nnp.cached_energy_ = e;
+  nnp.cached_ = true;
+}
+
+double NNP::energy(NNP& nnp, Structure& struc) {
+  if (!nnp.ctx_) throw std::runtime_error("NNP::energy: no potential read");
+  if (nnp.cached_ && nnp.cached_key_ == fingerprint(struc)) {
+    struc.energy() = nnp.cached_energy_;
+    return struc.energy();
+  }
+  const Structure* p = &struc;
+  Flat f;
+  flatten(nnp, &p, 1, f);
+  double e = 0.0;
+  const int flags = NNPGPU_ENERGY | (nnp.bf16_ ? NNPGPU_BF16 : 0);
+  check(nnp.ctx(), nnpgpu_compute(nnp.ctx(), 1, f.natoms.data(), f.posn.data(), f.species.data(), f.cell.data(), flags, &e, nullptr, nullptr),
+        "NNP::energy");
+  struc.energy() = e;
+  return e;
+}
+
+static void force_impl(NNP& nnp, Structure& struc, bool no_vacuum, const char* where) {
+  if (!nnp.ctx()) throw std::runtime_error(std::string(where) + ": no potential read");
+  const Structure* p = &struc;
+  Flat f;
+  flatten(nnp, &p, 1, f);
+  double e = 0.0;
+  std::vector<double> F(3 * (size_t)std::max(struc.nAtoms(), 1));
+  const int flags = NNPGPU_ENERGY | NNPGPU_FORCE | (no_vacuum ? NNPGPU_NO_VACUUM : 0) | (nnp.bf16() ? NNPGPU_BF16 : 0);
+  check(nnp.ctx(), nnpgpu_compute(nnp.ctx(), 1, f.natoms.data(), f.posn.data(), f.species.data(), f.cell.data(), flags, &e, F.data(), nullptr),
+        where);
+  for (int i = 0; i < struc.nAtoms(); ++i)
+    for (int x = 0; x < 3; ++x) struc.force(i)[x] = F[3 * (size_t)i + x];
+  if (no_vacuum) struc.energy() = e;
+}
+
+void NNP::force(NNP& nnp, Structure& struc, const NeighborList&) { force_impl(nnp, struc, false, "NNP::force"); }
+
+void NNP::compute(NNP& nnp, Structure& struc, const NeighborList&) { force_impl(nnp, struc, true, "NNP::compute"); }
+
+void NNP::compute(NNP& nnp, std::vector<Structure>& strucs, bool force, bool no_vacuum) {
+  if (!nnp.ctx_) throw std::runtime_error("NNP::compute: no potential read");
+  if (strucs.empty()) return;
+  std::vector<const Structure*> ptrs(strucs.size());
+  for (size_t s = 0; s < strucs.size(); ++s) ptrs[s] = &strucs[s];
+  Flat f;
+  flatten(nnp, ptrs.data(), (int)ptrs.size(), f);
+  std::vector<double> E(strucs.size()), F(force ? std::max<size_t>(f.posn.size(), 3) : 0);
+  const int flags = NNPGPU_ENERGY | NNPGPU_BATCHED | (force ? NNPGPU_FORCE : 0) | (no_vacuum ? NNPGPU_NO_VACUUM : 0) |
+                    (nnp.bf16_ ? NNPGPU_BF16 : 0);
+  check(nnp.ctx(), nnpgpu_compute(nnp.ctx(), (int)strucs.size(), f.natoms.data(), f.posn.data(), f.species.data(), f.cell.data(), flags,
+                                  E.data(), force ? F.data() : nullptr, nullptr),
+        "NNP::compute (batched)");
+  size_t a = 0;
+  for (size_t s = 0; s < strucs.size(); ++s) {
+    strucs[s].energy() = E[s];
+    for (int i = 0; i < strucs[s].nAtoms(); ++i, ++a)
+      if (force)
+        for (int x = 0; x < 3; ++x) strucs[s].force(i)[x] = F[3 * a + x];
+  }
+}
+
+// ------------------------------------------------------------------------------ NeighborList
+void NeighborList::build(const Structure& struc, double rc) {
+  std::shared_ptr<nnpgpu_ctx> c;
+  {
+    std::lock_guard<std::mutex> l(g_last_mu);
+    c = g_last.lock();
+  }
+  if (!c) throw std::runtime_error("NeighborList::build: read a potential (NNP::read) first; it provides the GPU context");
+  NNP tmp;
+  tmp.ctx_ = c;
+  build(tmp, struc, rc);
+}
+
+void NeighborList::build(const NNP& nnp, const Structure& struc, double rc) {
+  if (!nnp.ctx()) throw std::runtime_error("NeighborList::build: no potential read");
+  if (!(rc > 0)) throw std::invalid_argument("NeighborList::build: invalid cutoff");
+  const int n = struc.nAtoms();
+  std::vector<double> posn(3 * (size_t)std::max(n, 1));
+  for (int i = 0; i < n; ++i)
+    for (int x = 0; x < 3; ++x) posn[3 * (size_t)i + x] = struc.posn(i)[x];
+  std::vector<int> count(std::max(n, 1));
+  int cap = 64;
+  for (;;) {
+    std::vector<int> index((size_t)std::max(n, 1) * cap), shift((size_t)std::max(n, 1) * cap * 3);
+    std::vector<float> r((size_t)std::max(n, 1) * cap * 4);
+    std::vector<unsigned char> mn((size_t)std::max(n, 1) * cap);
+    const int code = nnpgpu_neighbors_rc(nnp.ctx(), rc, n, posn.data(), struc.R().data(), cap, count.data(), index.data(), r.data(),
+                                         mn.data(), shift.data());
+    if (code == NNPGPU_ERR_CAPACITY && cap < 1024) {
+      int need = cap;
+      for (int i = 0; i < n; ++i) need = std::max(need, count[i]);
+      cap = std::min(1024, (need + 31) / 32 * 32);
+      continue;
+    }
+    check(nnp.ctx(), code, "NeighborList::build");
+    rc_ = rc;
+    neigh_.assign(n, {});
+    for (int i = 0; i < n; ++i) {
+      neigh_[i].resize(count[i]);
+      for (int s = 0; s < count[i]; ++s) {
+        const size_t g = (size_t)i * cap + s;
+        Neighbor& nb = neigh_[i][s];
+        nb.index() = index[g];
+        nb.r() = Vec3d(r[4 * g], r[4 * g + 1], r[4 * g + 2]);
+        nb.dr() = r[4 * g + 3];
+        nb.min() = mn[g] != 0;
+        nb.cell() = {shift[3 * g], shift[3 * g + 1], shift[3 * g + 2]};
+      }
+    }
+    return;
+  }
+}
+
+// ------------------------------------------------------------------------------ readers
+namespace VASP {
+namespace POSCAR {
+// VASP::POSCAR::read (src/format/vasp_struc.cpp:51-200): title, scale, three lattice vectors
+// (one per line, each a column of R), species names, counts, a coordinate-mode line whose first
+// character 'D' selects direct coordinates, then one position per atom.  Direct positions are
+// mapped through the scaled lattice; Cartesian ones are multiplied by s_len only (the file's
+// scale factor applies to the lattice alone, as in the reference).
+void read(const char* file, Structure& struc, double s_len) {
+  std::ifstream in(file ? file : "");
+  if (!in) throw std::runtime_error(std::string("I/O Error: Could not open file: ") + (file ? file : "(null)"));
+  std::string line;
+  auto next = [&](const char* what) -> std::string {
+    if (!std::getline(in, line)) throw std::runtime_error(std::string("POSCAR ") + file + ": missing " + what);
+    return line;
+  };
+  next("title");
+  double scale = 0.0;
+  if (std::sscanf(next("scale").c_str(), "%lf", &scale) != 1) throw std::runtime_error(std::string("POSCAR ") + file + ": bad scale");
+  double lv[9];
+  for (int c = 0; c < 3; ++c)
+    if (std::sscanf(next("lattice vector").c_str(), "%lf %lf %lf", &lv[3 * c], &lv[3 * c + 1], &lv[3 * c + 2]) != 3)
+      throw std::runtime_error(std::string("POSCAR ") + file + ": bad lattice vector");
+  for (double& v : lv) v *= s_len * scale;
+  const std::vector<std::string> names = tokens(next("species names"));
+  const std::vector<std::string> numbers = tokens(next("species counts"));
+  if (names.size() != numbers.size()) throw std::runtime_error("Invalid number of species");
+  if (names.empty()) throw std::runtime_error("Invalid number of species");
+  std::vector<int> counts;
+  int total = 0;
+  for (const std::string& t : numbers) {
+    counts.push_back(std::atoi(t.c_str()));
+    total += counts.back();
+  }
+  const bool direct = !next("coordinate mode").empty() && line[0] == 'D';
+  struc.clear();
+  struc.init(lv);
+  struc.resize(total);
+  for (int n = 0; n < total; ++n) {
+    double p[3];
+    if (std::sscanf(next("position").c_str(), "%lf %lf %lf", &p[0], &p[1], &p[2]) != 3)
+      throw std::runtime_error(std::string("POSCAR ") + file + ": bad position line " + std::to_string(n));
+    for (int x = 0; x < 3; ++x)
+      struc.posn(n)[x] = direct ? lv[x] * p[0] + lv[3 + x] * p[1] + lv[6 + x] * p[2] : p[x] * s_len;
+  }
+  int a = 0;
+  for (size_t s = 0; s < names.size(); ++s)
+    for (int m = 0; m < counts[s]; ++m, ++a) struc.name(a) = names[s];
+}
+}  // namespace POSCAR
+}  // namespace VASP
+
+namespace XYZ {
+// XYZ::read (src/format/xyz_struc.cpp:38-130): atom count; a line "<tag> energy" or
+// "<tag> energy a b c" (orthorhombic lattice lengths); then "name x y z" per atom.
+void read(const char* file, Structure& struc, double s_len, double s_energy) {
+  std::ifstream in(file ? file : "");
+  if (!in) throw std::runtime_error(std::string("ERROR in XYZ::read: Could not open file: ") + (file ? file : "(null)"));
+  std::string line;
+  if (!std::getline(in, line)) throw std::runtime_error(std::string("XYZ ") + file + ": empty file");
+  const int n = std::atoi(line.c_str());
+  if (n <= 0) throw std::runtime_error("ERROR in XYZ::read: found zero atoms.");
+  if (!std::getline(in, line)) throw std::runtime_error(std::string("XYZ ") + file + ": missing comment line");
+  const std::vector<std::string> t = tokens(line);
+  double energy = 0.0, lv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  if (t.size() == 2) {
+    energy = std::atof(t[1].c_str());
+  } else if (t.size() == 5) {
+    energy = std::atof(t[1].c_str());
+    lv[0] = std::atof(t[2].c_str()) * s_len;
+    lv[4] = std::atof(t[3].c_str()) * s_len;
+    lv[8] = std::atof(t[4].c_str()) * s_len;
+  }
+  struc.clear();
+  struc.resize(n);
+  for (int i = 0; i < n; ++i) {
+    if (!std::getline(in, line)) throw std::runtime_error(std::string("XYZ ") + file + ": missing atom line " + std::to_string(i));
+    char name[256];
+    double p[3];
+    if (std::sscanf(line.c_str(), "%255s %lf %lf %lf", name, &p[0], &p[1], &p[2]) != 4)
+      throw std::runtime_error(std::string("XYZ ") + file + ": bad atom line " + std::to_string(i));
+    struc.name(i) = name;
+    for (int x = 0; x < 3; ++x) struc.posn(i)[x] = p[x] * s_len;
+  }
+  struc.init(lv);
+  struc.energy() = s_energy * energy;
+}
+}  // namespace XYZ
+
+// ------------------------------------------------------------------------------ parameters
+bool boolean(const std::string& s) {
+  return s == "T" || s == "t" || s == "TRUE" || s == "true" || s == "True" || s == "1";
+}
+
+ComputeParams read_compute_params(const char* file) {
+  std::ifstream in(file ? file : "");
+  if (!in) throw std::runtime_error("I/O Error: could not open parameter file.");
+  ComputeParams p;
+  std::string line;
+  while (std::getline(in, line)) {
+    const std::vector<std::string> t = tokens(line);
+    if (t.empty()) continue;
+    const std::string tag = upper(t[0]);
+    const std::string val = t.size() > 1 ? t[1] : "";
+    if (tag == "DATA") p.data.push_back(val);
+    else if (tag == "NNPOT") p.nnpot = val;
+    else if (tag == "FORMAT") p.format = upper(val);
+    else if (tag == "UNITS") p.units = upper(val);
+    else if (tag == "FORCE") p.force = boolean(val);
+    else if (tag == "NORM") p.norm = boolean(val);
+    else if (tag == "BF16") p.bf16 = boolean(val);
+    else if (tag == "BATCH") p.batch_atoms = std::max(1LL, std::atoll(val.c_str()));
+  }
+  if (p.units != "METAL" && p.units != "AU") throw std::invalid_argument("Invalid unit system.");
+  if (p.format != "POSCAR" && p.format != "XYZ") throw std::invalid_argument("Invalid file format.");
+  if (p.data.empty()) throw std::invalid_argument("No data");
+  return p;
+}
+
+std::vector<std::string> read_data_lists(const std::vector<std::string>& data) {
+  std::vector<std::string> files;
+  for (const std::string& d : data) {
+    std::ifstream in(d);
+    if (!in) throw std::runtime_error("I/O Error: Could not open data file: " + d);
+    std::string line;
+    while (std::getline(in, line)) {
+      const size_t a = line.find_first_not_of(" \t\r\n");
+      if (a == std::string::npos) continue;
+      const size_t b = line.find_last_not_of(" \t\r\n");
+      files.push_back(line.substr(a, b - a + 1));
+    }
+  }
+  return files;
+}
+
+}  // namespace atomnn_gpu

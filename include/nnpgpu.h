@@ -90,6 +90,12 @@ int nnpgpu_compute_device(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const 
 int nnpgpu_neighbors(nnpgpu_ctx* ctx, int natoms, const double* posn, const double* cell, int cap,
                      int* count, int* index, float* r, unsigned char* min, int* shift);
 
+/* The same at an explicit cutoff rc > 0 (NeighborList::build(const Structure&, double rc),
+ * src/struc/neighbor.hpp:85, whose cutoff is the caller's and need not be the potential's), with
+ * up to 1024 entries per atom.  The context only provides the device and its stream. */
+int nnpgpu_neighbors_rc(nnpgpu_ctx* ctx, double rc, int natoms, const double* posn, const double* cell,
+                        int cap, int* count, int* index, float* r, unsigned char* min, int* shift);
+
 /* ---- symmetry functions without device allocation.  No counterpart in the reference (AtomNN
  * allocates through Eigen on every call).  For callers that cannot let a library allocate device
  * memory while they run: codes that divide the GPU's memory among their own pools before the

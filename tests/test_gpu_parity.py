@@ -136,6 +136,46 @@ def test_edge_cases_against_oracle(engines, oracles, case):
     _assert_ef(e[0], F[0], eo, Fo, s.natoms)
 
 
+def _dense_cell(n, rho, seed, angles=(84.0, 97.0, 91.0), wrap=True):
+    rng = np.random.default_rng(seed)
+    L = (n / rho) ** (1.0 / 3.0)
+    cell = W.lattice(L, 1.05 * L, 0.95 * L, *angles)
+    f = rng.uniform(0, 1, size=(n, 3))
+    if not wrap:  # positions several cells away from the home cell
+        f += rng.integers(-3, 4, size=(n, 3))
+    return W.Structure(posn=f @ cell.T, species=(rng.uniform(size=n) < 0.33).astype(np.int32), cell=cell)
+
+
+@pytest.mark.parametrize("case", ["n300", "n700", "n2048", "unwrapped", "lattice_ties", "n5000"])
+def test_cell_list_neighbors(engines, case):
+    """Structures large enough for the cell-list build (reach 1-3 cells, stencils that wrap,
+    positions outside the home cell, atoms exactly on cell faces, more than 4096 atoms): the
+    lists equal the oracle's, order and minimum-image flags included."""
+    if case == "lattice_ties":
+        m, a = 12, 2.2  # 12 cells per axis at reach 3: every atom sits on a cell face
+        idx = np.array([(x, y, z) for x in range(m) for y in range(m) for z in range(m)], dtype=float)
+        s = W.Structure(posn=idx * a, species=(np.arange(m ** 3) % 2).astype(np.int32), cell=np.eye(3) * m * a)
+    elif case == "unwrapped":
+        s = _dense_cell(900, 0.07, 5, wrap=False)
+    else:
+        n = int(case[1:])
+        s = _dense_cell(n, {300: 0.09, 700: 0.05, 2048: 0.07, 5000: 0.06}[n], n)
+    from oracle import pyoracle
+    rc = engines["mixed512"].rc
+    _assert_lists_equal(engines["mixed512"].neighbors(s.posn, s.cell), pyoracle.neighbors(rc, s.posn, s.cell))
+
+
+def test_cell_list_batch_against_oracle(engines, oracles):
+    """A batch mixing image-shell, brute-force and cell-list structures: energies and forces.
+    (Workload structures: uniform random positions put atoms 0.3 A apart, where FP32 forces
+    are not meant to hold 1e-4 eV/A.)"""
+    strucs = W.make_structures("mixed512", seed=40, count=4, sizes=[40, 180, 1100, 2048])
+    e, F, _ = engines["mixed512"].compute(strucs, _flags("ENERGY", "FORCE", "BATCHED"))
+    for k, s in enumerate(strucs):
+        eo, Fo, _ = oracles["mixed512"].compute(s.posn, s.species, s.cell, force=True)
+        _assert_ef(e[k], F[k], eo, Fo, s.natoms)
+
+
 def test_empty_structures_in_batch(engines, oracles):
     strucs = W.make_structures("mixed512", seed=8, count=3, sizes=[20, 30, 25])
     empty = W.Structure(posn=np.zeros((0, 3)), species=np.zeros(0, np.int32), cell=np.eye(3) * 10)
