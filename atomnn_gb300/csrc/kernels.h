@@ -50,16 +50,19 @@ struct BatchDev {
   int* status = nullptr;   // [ST_WORDS]
 };
 
-// Launch configuration chosen by the autotuner (atoms per CTA for the triplet kernels).
+// Launch shapes chosen by the autotuner (nnpgpu_autotune): centre atoms (warps) per CTA of
+// the neighbour, descriptor and chain-rule kernels, and the atom tile of the FP32 networks.
 struct TuneCfg {
+  int warps_nbr = 4;
   int warps_symm = 4;
   int warps_force = 4;
   int nn_tile = 32;
 };
 
-void launch_neighbors(const BatchDev& B, cudaStream_t st);
+// warps = centre atoms per CTA (1-4)
+void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps = 4);
 // dynamic shared memory of the neighbour kernel when some structure uses a cell list
-size_t neighbor_smem_bytes(int cap);
+size_t neighbor_smem_bytes(int cap, int warps);
 void launch_reverse(const BatchDev& B, cudaStream_t st);
 // descriptors (NNP::symm) and chain rule (NNP::force) ; ne/nz select the template instance
 int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);

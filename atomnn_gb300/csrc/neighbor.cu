@@ -212,7 +212,7 @@ __device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& s
 constexpr int NB_RANGES = 128;  // >= 2 (2*3+1)^2 rows of the widest stencil (reach 3)
 constexpr int NB_MASK_WORDS = 128;  // structures up to 4096 atoms rank through the bit mask
 __host__ __device__ inline size_t nb_warp_smem(int cap) { return (size_t)cap * 24 + 4 * (2 * NB_RANGES + 2 * NB_MASK_WORDS); }
-size_t neighbor_smem_bytes(int cap) { return 4 * nb_warp_smem(cap); }
+size_t neighbor_smem_bytes(int cap, int warps) { return (size_t)warps * nb_warp_smem(cap); }
 
 __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int cap, double rc, const double* __restrict__ posn,
                                                        const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
@@ -594,7 +594,8 @@ __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int ca
   }
 }
 
-void launch_neighbors(const BatchDev& B, cudaStream_t st) {
+void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
+  warps = warps < 1 ? 1 : (warps > 4 ? 4 : warps);
   if (B.natoms == 0) return;
   frac_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.ntypes, B.type, B.posn, B.atom_struc, B.meta, B.sfrac,
                                                       B.sfloor, B.atom_cell, B.cell_cnt, B.status);
@@ -603,12 +604,12 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st) {
     cell_scan_kernel<<<B.nstruc, 256, 0, st>>>(B.s0, B.meta, B.cell_cnt, B.cell_start);
     cell_fill_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.atom_struc, B.meta, B.atom_cell, B.cell_cnt, B.cell_start,
                                                              B.cell_atoms);
-    smem = neighbor_smem_bytes(B.cap);
+    smem = neighbor_smem_bytes(B.cap, warps);
     static bool attr = false;  // skin lists may ask for up to 1024 slots per atom (106 KB)
     if (!attr) attr = cudaFuncSetAttribute(neighbor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   }
-  const int blocks = (B.natoms + 3) / 4;
-  neighbor_kernel<<<blocks, 128, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
+  const int blocks = (B.natoms + warps - 1) / warps;
+  neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
                                              B.atom_cell, B.cell_start, B.cell_atoms, B.nb_j, B.nb_r, B.nb_code, B.nb_cnt, B.status);
 }
 

@@ -3,14 +3,12 @@
 // NNH::energy, src/nnp/nnh.cpp:127-130).
 //
 // Atoms are grouped by species first (type_sort), so each CTA runs one network over a tile of
-// TILE atoms: every layer is an (atoms x in) x (in x out) product with activations staged
-// transposed in shared memory and weights streamed from L2.
+// TILE atoms (16, 32 or 64, chosen by the autotuner): every layer is an (atoms x in) x (in x out)
+// product with activations staged transposed in shared memory and weights streamed from L2.
 #include "common.cuh"
 #include "kernels.h"
 
 namespace nnpgpu {
-
-constexpr int TILE = 32;
 
 __global__ void type_count_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, int* __restrict__ tc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -57,9 +55,10 @@ __device__ __forceinline__ void act_fd(int act, float z, float& a, float& d) {
 
 // out[n][t] = sum_k inT[k][t] * B[k*ldb + n] for t < TILE, n < N; inT is [K][TILE] in smem.
 // Each thread owns one output column n and 16 atoms.
+template <int TILE>
 __device__ __forceinline__ void tile_gemm(const float* __restrict__ inT, int K, const float* __restrict__ Bm, int ldb, int N,
                                           float* __restrict__ outT, const float* __restrict__ bias) {
-  for (int w = threadIdx.x; w < N * 2; w += blockDim.x) {
+  for (int w = threadIdx.x; w < N * (TILE / 16); w += blockDim.x) {
     const int n = w % N, h = w / N;
     float acc[16];
 #pragma unroll
@@ -82,6 +81,7 @@ __device__ __forceinline__ void tile_gemm(const float* __restrict__ inT, int K, 
   }
 }
 
+template <int TILE>
 __global__ void __launch_bounds__(128) network_fp32_kernel(const __grid_constant__ NetsP N, int ntypes, const int* __restrict__ tc,
                                                            const int* __restrict__ perm, const float* __restrict__ G, int gstride,
                                                            float* __restrict__ eatom, float* __restrict__ dEdG, int want_grad) {
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(128) network_fp32_kernel(const __grid_constant
   const float* in = XT;
   int Kl = K0;
   for (int l = 0; l < L - 1; ++l) {
-    tile_gemm(in, Kl, net.wt[l], net.nodes[l], net.nodes[l], A[l], net.b[l]);
+    tile_gemm<TILE>(in, Kl, net.wt[l], net.nodes[l], net.nodes[l], A[l], net.b[l]);
     __syncthreads();
     for (int w = threadIdx.x; w < net.nodes[l] * TILE; w += blockDim.x) {
       float a, d;
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(128) network_fp32_kernel(const __grid_constant
   }
   for (int l = L - 2; l >= 1; --l) {
     // gnext[c][t] = sum_r gcur[r][t] W_l[r][c]
-    tile_gemm(gcur, net.nodes[l], net.w[l], net.nodes[l - 1], net.nodes[l - 1], gnext, nullptr);
+    tile_gemm<TILE>(gcur, net.nodes[l], net.w[l], net.nodes[l - 1], net.nodes[l - 1], gnext, nullptr);
     __syncthreads();
     for (int w = threadIdx.x; w < net.nodes[l - 1] * TILE; w += blockDim.x) {
       const float a = A[l - 1][w];
@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(128) network_fp32_kernel(const __grid_constant
     float* tmp = gcur; gcur = gnext; gnext = tmp;
   }
   // dodi = (g_0 W_0) .* inpw -> dE/dG
-  tile_gemm(gcur, net.nodes[0], net.w[0], K0, K0, gnext, nullptr);
+  tile_gemm<TILE>(gcur, net.nodes[0], net.w[0], K0, K0, gnext, nullptr);
   __syncthreads();
   for (int w = threadIdx.x; w < K0 * TILE; w += blockDim.x) {
     const int k = w / TILE, a = w % TILE;
@@ -175,8 +175,8 @@ __global__ void __launch_bounds__(128) network_fp32_kernel(const __grid_constant
   }
 }
 
-void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int /*tile*/, cudaStream_t st) {
-  if (B.natoms == 0) return;
+template <int TILE>
+static void launch_network_fp32_t(const BatchDev& B, const NetsP& N, int ntypes, cudaStream_t st) {
   size_t floats = 0;
   for (int t = 0; t < ntypes; ++t) {
     const NetP& n = N.net[t];
@@ -187,10 +187,17 @@ void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int /*ti
     floats = max(floats, f);
   }
   static bool attr = false;
-  if (!attr) attr = cudaFuncSetAttribute(network_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  if (!attr) attr = cudaFuncSetAttribute(network_fp32_kernel<TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   const int tiles = (B.natoms + TILE - 1) / TILE + ntypes;
-  network_fp32_kernel<<<tiles, 128, floats * sizeof(float), st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride, B.eatom,
-                                                                   B.dEdG, 1);
+  network_fp32_kernel<TILE><<<tiles, 128, floats * sizeof(float), st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride, B.eatom,
+                                                                         B.dEdG, 1);
+}
+
+void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile, cudaStream_t st) {
+  if (B.natoms == 0) return;
+  if (tile <= 16) launch_network_fp32_t<16>(B, N, ntypes, st);
+  else if (tile <= 32) launch_network_fp32_t<32>(B, N, ntypes, st);
+  else launch_network_fp32_t<64>(B, N, ntypes, st);
 }
 
 }  // namespace nnpgpu

@@ -211,7 +211,7 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
     if (prof) cudaEventRecordWithFlags(c->prof_ev[k], st, ev_flags);
   };
   mark(0);
-  launch_neighbors(B, st);
+  launch_neighbors(B, st, c->tune.warps_nbr);
   mark(1);
   if (want_force) launch_reverse(B, st);
   mark(2);
@@ -778,6 +778,104 @@ static int neighbors_impl(nnpgpu_ctx* c, double rc_req, int max_slots, int natom
   if (status == NNPGPU_OK && hstat[ST_MAXCOUNT] > U.cap)
     status = set_error(c, NNPGPU_ERR_CAPACITY, "neighbour list longer than " + std::to_string(max_slots));
   return status;
+}
+
+// Launch-shape autotuner.  Coordinate descent over the knobs of TuneCfg: each candidate value is
+// timed on the caller's batch from the stage events recorded inside the captured launch
+// sequence (best of `reps` graph replays after a warm-up run and the capture run), and the
+// fastest value is kept before the next knob is tried.
+static int tune_stage(nnpgpu_ctx* c, int* knob, const int* cand, int ncand, int stage, int nstruc, const int* natoms, const double* posn,
+                      const int* species, const double* cell, int flags, double* energy, double* force, std::string& rep,
+                      const char* name) {
+  const int keep = *knob;
+  int best = keep;
+  double best_ms = 1e30;
+  char buf[64];
+  rep += name;
+  rep += " {";
+  for (int k = 0; k < ncand; ++k) {
+    *knob = cand[k];
+    drop_graphs(c);
+    c->shapes_seen.clear();
+    for (int w = 0; w < 2; ++w) {  // first run of the shape, then the captured run
+      const int rc = compute_impl(c, nstruc, natoms, posn, species, cell, flags, energy, force, nullptr, false, nullptr);
+      if (rc != NNPGPU_OK) { *knob = keep; return rc; }
+    }
+    double ms = 1e30;
+    for (int r = 0; r < 3; ++r) {
+      c->prof_ms[stage] = 0;
+      c->prof_n[stage] = 0;
+      const int rc = compute_impl(c, nstruc, natoms, posn, species, cell, flags, energy, force, nullptr, false, nullptr);
+      if (rc != NNPGPU_OK) { *knob = keep; return rc; }
+      if (c->prof_n[stage] > 0) ms = std::min(ms, c->prof_ms[stage] / (double)c->prof_n[stage]);
+    }
+    std::snprintf(buf, sizeof(buf), "%s%d: %.4f ms", k ? ", " : "", cand[k], ms);
+    rep += buf;
+    if (ms < best_ms) { best_ms = ms; best = cand[k]; }
+  }
+  *knob = best;
+  std::snprintf(buf, sizeof(buf), "} -> %d; ", best);
+  rep += buf;
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_autotune(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
+                               int flags, char* report, int report_len) {
+  if (!c || nstruc <= 0 || !natoms || !posn || !species || !cell) return set_error(c, NNPGPU_ERR_INVALID, "invalid arguments");
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  flags = (flags & (NNPGPU_BF16 | NNPGPU_FORCE | NNPGPU_NO_VACUUM)) | NNPGPU_ENERGY | NNPGPU_BATCHED;
+  size_t total = 0;
+  for (int s = 0; s < nstruc; ++s) total += natoms[s] > 0 ? natoms[s] : 0;
+  std::vector<double> energy(nstruc), force((flags & NNPGPU_FORCE) ? 3 * std::max<size_t>(total, 1) : 0);
+  double* fp = (flags & NNPGPU_FORCE) ? force.data() : nullptr;
+  const bool was_on = c->prof_on;
+  int rc = nnpgpu_profile_enable(c, 1);
+  if (rc != NNPGPU_OK) return rc;
+  std::string rep;
+  static const int warps[] = {1, 2, 4};
+  static const int tiles[] = {16, 32, 64};
+  rc = tune_stage(c, &c->tune.warps_nbr, warps, 3, 0, nstruc, natoms, posn, species, cell, flags, energy.data(), fp, rep, "warps_nbr");
+  if (rc == NNPGPU_OK)
+    rc = tune_stage(c, &c->tune.warps_symm, warps, 3, 2, nstruc, natoms, posn, species, cell, flags, energy.data(), fp, rep, "warps_symm");
+  if (rc == NNPGPU_OK && !(flags & NNPGPU_BF16))
+    rc = tune_stage(c, &c->tune.nn_tile, tiles, 3, 3, nstruc, natoms, posn, species, cell, flags, energy.data(), fp, rep, "nn_tile");
+  if (rc == NNPGPU_OK && (flags & NNPGPU_FORCE))
+    rc = tune_stage(c, &c->tune.warps_force, warps, 3, 4, nstruc, natoms, posn, species, cell, flags, energy.data(), fp, rep, "warps_force");
+  const std::string err = c->err;
+  nnpgpu_profile_enable(c, was_on ? 1 : 0);  // also drops the graphs captured while tuning
+  drop_graphs(c);
+  c->shapes_seen.clear();
+  if (rc != NNPGPU_OK) {
+    c->err = err;
+    return rc;
+  }
+  if (report && report_len > 0) {
+    std::snprintf(report, (size_t)report_len, "%s", rep.c_str());
+  }
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_get_tune(const nnpgpu_ctx* c, int* warps_nbr, int* warps_symm, int* warps_force, int* nn_tile) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (warps_nbr) *warps_nbr = c->tune.warps_nbr;
+  if (warps_symm) *warps_symm = c->tune.warps_symm;
+  if (warps_force) *warps_force = c->tune.warps_force;
+  if (nn_tile) *nn_tile = c->tune.nn_tile;
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_set_tune(nnpgpu_ctx* c, int warps_nbr, int warps_symm, int warps_force, int nn_tile) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  auto ok_w = [](int w) { return w == 1 || w == 2 || w == 4; };
+  if (!ok_w(warps_nbr) || !ok_w(warps_symm) || !ok_w(warps_force) || !(nn_tile == 16 || nn_tile == 32 || nn_tile == 64))
+    return set_error(c, NNPGPU_ERR_INVALID, "launch shapes: warps 1, 2 or 4; FP32 network tile 16, 32 or 64");
+  c->tune.warps_nbr = warps_nbr;
+  c->tune.warps_symm = warps_symm;
+  c->tune.warps_force = warps_force;
+  c->tune.nn_tile = nn_tile;
+  drop_graphs(c);  // captured sequences hold the old shapes
+  c->shapes_seen.clear();
+  return NNPGPU_OK;
 }
 
 extern "C" int nnpgpu_neighbors(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, int cap, int* count, int* index,

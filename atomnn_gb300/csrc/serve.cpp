@@ -288,6 +288,7 @@ Serving::Serving(nnpgpu_ctx* c, const nnpgpu_serve_opts& o) : impl_(new Impl) {
       if (sc) nnpgpu_destroy(sc);
       throw PotError(rc, "could not create a serving slot");
     }
+    sc->tune = c->tune;  // slots run with the owner's (possibly autotuned) launch shapes
     I.slots.push_back(sc);
   }
   for (int s = 0; s < I.opts.max_inflight; ++s) I.threads.emplace_back([this, s] { impl_->worker(s); });

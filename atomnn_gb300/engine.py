@@ -18,7 +18,7 @@ ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
-           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc"]
+           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune"]
 
 _lib = None
 
@@ -62,6 +62,9 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_compute_device.argtypes = [vp, ip, vp, vp, vp, vp, ip, vp, vp, vp, vp]
     L.nnpgpu_neighbors.argtypes = [vp, ip, vp, vp, ip, vp, vp, vp, vp, vp]
     L.nnpgpu_neighbors_rc.argtypes = [vp, dp, ip, vp, vp, ip, vp, vp, vp, vp, vp]
+    L.nnpgpu_autotune.argtypes = [vp, ip, vp, vp, vp, vp, ip, ctypes.c_char_p, ip]
+    L.nnpgpu_get_tune.argtypes = [vp, vp, vp, vp, vp]
+    L.nnpgpu_set_tune.argtypes = [vp, ip, ip, ip, ip]
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
     L.nnpgpu_submit.argtypes = [vp, ip, vp, vp, vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
     L.nnpgpu_poll.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.POINTER(ctypes.c_double)]
@@ -157,6 +160,24 @@ class Engine:
         cellc = _cell_colmajor(cell)
         self._check(self.lib.nnpgpu_symm_noalloc(self._ctx, natoms, ctypes.c_void_p(d_posn or None), ctypes.c_void_p(d_species or None),
                                                  _p(cellc), ctypes.c_void_p(d_symm or None), symm_stride, ctypes.c_void_p(stream or None)))
+
+    # ---- launch-shape autotuner
+    def autotune(self, natoms, posn, species, cells_colmajor, flags=FORCE):
+        """nnpgpu_autotune on pre-packed host arrays; returns (shapes dict, report string)."""
+        buf = ctypes.create_string_buffer(4096)
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        self._check(self.lib.nnpgpu_autotune(self._ctx, len(natoms), _p(natoms), _p(np.ascontiguousarray(posn, dtype=np.float64)),
+                                             _p(np.ascontiguousarray(species, dtype=np.int32)),
+                                             _p(np.ascontiguousarray(cells_colmajor, dtype=np.float64)), flags, buf, len(buf)))
+        return self.get_tune(), buf.value.decode()
+
+    def get_tune(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        self._check(self.lib.nnpgpu_get_tune(self._ctx, *[ctypes.byref(x) for x in v]))
+        return dict(zip(("warps_nbr", "warps_symm", "warps_force", "nn_tile"), (x.value for x in v)))
+
+    def set_tune(self, warps_nbr=4, warps_symm=4, warps_force=4, nn_tile=32):
+        self._check(self.lib.nnpgpu_set_tune(self._ctx, warps_nbr, warps_symm, warps_force, nn_tile))
 
     # ---- serving (continuous batching)
     def serve_start(self, max_batch_atoms=0, max_inflight=2, hbm_budget_bytes=0, skin=1.0, flags=0):

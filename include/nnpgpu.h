@@ -120,6 +120,19 @@ int nnpgpu_profile_enable(nnpgpu_ctx* ctx, int on);
 int nnpgpu_profile_read(const nnpgpu_ctx* ctx, int stage, double* total_ms, long long* count);
 const char* nnpgpu_profile_stage_name(int stage);
 
+/* ---- launch-shape autotuner (no counterpart in the reference, which has no launch shapes).
+ * Times the batched path on the given batch (host buffers, as nnpgpu_compute) for each candidate
+ * of each knob - centre atoms (warps) per CTA of the neighbour, descriptor and chain-rule kernels
+ * (1, 2, 4) and the atom tile of the FP32 networks (16, 32, 64; skipped with NNPGPU_BF16) - one
+ * knob at a time, from stage events inside the captured launch sequence, and keeps the fastest.
+ * flags: NNPGPU_BF16, NNPGPU_FORCE (the chain-rule knob is tuned only with it).  report (may be
+ * NULL) receives the per-candidate times.  Later calls of the context use the chosen shapes;
+ * nnpgpu_get_tune / nnpgpu_set_tune read and restore them (e.g. from a caller's cache). */
+int nnpgpu_autotune(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* posn, const int* species,
+                    const double* cell, int flags, char* report, int report_len);
+int nnpgpu_get_tune(const nnpgpu_ctx* ctx, int* warps_nbr, int* warps_symm, int* warps_force, int* nn_tile);
+int nnpgpu_set_tune(nnpgpu_ctx* ctx, int warps_nbr, int warps_symm, int warps_force, int nn_tile);
+
 /* ---- serving: continuous batching of energy+force requests (no counterpart in the
  * reference, whose compute tool evaluates a fixed file list; it serves the same call as
  * nnpgpu_compute for requests that arrive over time). */

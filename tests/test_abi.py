@@ -76,3 +76,22 @@ def test_no_gpu_fails_loudly(native_lib, pot_small64):
     with pytest.raises(engine.NNPGPUError) as ei:
         engine.Engine(pot_small64)
     assert ei.value.code == engine.ERR_CUDA
+
+
+def test_tune_shapes_validated(native_lib):
+    """nnpgpu_set_tune accepts only the shapes the kernels are built for, and nnpgpu_get_tune
+    reads back what was set; a context without a device still holds its settings."""
+    from atomnn_gb300 import engine
+    ctx = ctypes.c_void_p()
+    native_lib.nnpgpu_create(os.path.join(GOLDEN, "small64.nnp").encode(), None, ctypes.byref(ctx))
+    assert ctx
+    try:
+        assert native_lib.nnpgpu_set_tune(ctx, 3, 4, 4, 32) == engine.ERR_INVALID
+        assert native_lib.nnpgpu_set_tune(ctx, 4, 4, 4, 48) == engine.ERR_INVALID
+        assert native_lib.nnpgpu_set_tune(ctx, 2, 1, 4, 64) == engine.OK
+        v = [ctypes.c_int() for _ in range(4)]
+        assert native_lib.nnpgpu_get_tune(ctx, *[ctypes.byref(x) for x in v]) == engine.OK
+        assert [x.value for x in v] == [2, 1, 4, 64]
+        assert native_lib.nnpgpu_autotune(ctx, 0, None, None, None, None, 0, None, 0) == engine.ERR_INVALID
+    finally:
+        native_lib.nnpgpu_destroy(ctx)

@@ -269,3 +269,30 @@ def test_bf16_networks_mixed_batch(engines, oracles):
         assert np.sqrt(((F[k] - Fo) ** 2).mean()) <= BF16_F_RMSE
         # and the BF16 path really differs from the FP32 one (the tensor-core kernel ran)
         assert not np.array_equal(F[k], F32[k])
+
+
+def test_autotune_keeps_results(native_lib):
+    """The autotuner times every candidate launch shape on a batch and keeps the fastest; launch
+    shapes do not change any atom's arithmetic, so results are bit-identical before and after."""
+    from atomnn_gb300 import engine
+    eng = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"))
+    try:
+        strucs = W.make_structures("mixed512", seed=55, count=16)
+        flags = _flags("ENERGY", "FORCE", "BATCHED")
+        e0, F0, _ = eng.compute(strucs, flags)
+        natoms = np.array([s.natoms for s in strucs], np.int32)
+        posn = np.concatenate([s.posn for s in strucs])
+        spec = np.concatenate([s.species for s in strucs]).astype(np.int32)
+        cells = np.concatenate([s.cell_colmajor() for s in strucs])
+        shapes, report = eng.autotune(natoms, posn, spec, cells, engine.FORCE)
+        for knob in ("warps_nbr", "warps_symm", "nn_tile", "warps_force"):
+            assert knob in report
+        assert shapes["warps_nbr"] in (1, 2, 4) and shapes["warps_force"] in (1, 2, 4) and shapes["nn_tile"] in (16, 32, 64)
+        for tune in (shapes, dict(warps_nbr=1, warps_symm=2, warps_force=1, nn_tile=64)):
+            eng.set_tune(**tune)
+            e1, F1, _ = eng.compute(strucs, flags)
+            np.testing.assert_array_equal(e0, e1)
+            for a, b in zip(F0, F1):
+                np.testing.assert_array_equal(a, b)
+    finally:
+        eng.close()
