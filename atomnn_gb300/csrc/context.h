@@ -91,7 +91,10 @@ int compute_host(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* pos
 // Builds the neighbour list of one structure with cutoff rc_skin into device arrays of skin_cap
 // slots per atom (local atom indices).  Returns OK, or NNPGPU_ERR_CAPACITY with *max_count set.
 int build_skin(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, double rc_skin, int skin_cap, int* d_j, int* d_code,
-               int* d_cnt, float4* d_r, int* max_count);
+               int* d_cnt, float4* d_r, int* max_count, bool posn_on_device = false);
+// Device-buffer evaluation (as nnpgpu_compute_device) with optional resident skin lists.
+int compute_device_skins(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* d_posn, const int* d_species, const double* cell,
+                         int flags, double* d_energy, double* d_force, cudaStream_t st, const SkinRef* skins);
 // Packs the BF16 weights of the tensor-core network path (network_tc.cu).
 int prepare_tc_weights(nnpgpu_ctx* c);
 }  // namespace nnpgpu

@@ -684,8 +684,13 @@ int compute_host(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* pos
   return compute_impl(c, nstruc, natoms, posn, species, cell, flags, energy, force, symm, false, nullptr, skins);
 }
 
+int compute_device_skins(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* d_posn, const int* d_species, const double* cell,
+                         int flags, double* d_energy, double* d_force, cudaStream_t st, const SkinRef* skins) {
+  return compute_impl(c, nstruc, natoms, d_posn, d_species, cell, flags, d_energy, d_force, nullptr, true, st, skins);
+}
+
 int build_skin(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell, double rc_skin, int skin_cap, int* d_j, int* d_code,
-               int* d_cnt, float4* d_r, int* max_count) {
+               int* d_cnt, float4* d_r, int* max_count, bool posn_on_device) {
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;
   *max_count = 0;
@@ -696,7 +701,7 @@ int build_skin(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell
   int rc = prepare(c, 1, &natoms, cell, skin_cap, U, st);
   c->pot.rc = saved;
   if (rc != NNPGPU_OK) return rc;
-  cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * natoms, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * natoms, posn_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
   BatchDev B = batch_view(c, U, (const double*)c->posn.p, nullptr, (double*)c->energy.p, (double*)c->force.p);
   B.rc = rc_skin;
   B.nb_j = d_j;

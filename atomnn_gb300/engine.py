@@ -18,7 +18,8 @@ ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
-           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune"]
+           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
+           "nnpgpu_md_state", "nnpgpu_md_destroy"]
 
 _lib = None
 
@@ -65,6 +66,12 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_autotune.argtypes = [vp, ip, vp, vp, vp, vp, ip, ctypes.c_char_p, ip]
     L.nnpgpu_get_tune.argtypes = [vp, vp, vp, vp, vp]
     L.nnpgpu_set_tune.argtypes = [vp, ip, ip, ip, ip]
+    L.nnpgpu_md_create.argtypes = [vp, ip, vp, vp, vp, vp, vp, dp, dp, ip, ctypes.POINTER(vp)]
+    L.nnpgpu_md_forces.argtypes = [vp, vp]
+    L.nnpgpu_md_run.argtypes = [vp, ip, vp, vp]
+    L.nnpgpu_md_state.argtypes = [vp, vp, vp, vp, vp]
+    L.nnpgpu_md_destroy.argtypes = [vp]
+    L.nnpgpu_md_destroy.restype = None
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
     L.nnpgpu_submit.argtypes = [vp, ip, vp, vp, vp, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)]
     L.nnpgpu_poll.argtypes = [vp, ctypes.c_longlong, vp, vp, ctypes.POINTER(ctypes.c_double)]
@@ -179,6 +186,11 @@ class Engine:
     def set_tune(self, warps_nbr=4, warps_symm=4, warps_force=4, nn_tile=32):
         self._check(self.lib.nnpgpu_set_tune(self._ctx, warps_nbr, warps_symm, warps_force, nn_tile))
 
+    # ---- molecular dynamics on resident device state
+    def md(self, struc, mass, dt, skin=1.0, vel=None, flags=0):
+        """An MD run of one structure (nnpgpu_md_*); mass per atom.  Returns an MD object."""
+        return MD(self, struc, mass, dt, skin, vel, flags)
+
     # ---- serving (continuous batching)
     def serve_start(self, max_batch_atoms=0, max_inflight=2, hbm_budget_bytes=0, skin=1.0, flags=0):
         o = ServeOpts(max_batch_atoms, max_inflight, hbm_budget_bytes, skin, flags)
@@ -236,3 +248,40 @@ class Engine:
                                                      _p(index), _p(r), _p(mn), _p(sh)))
         return [dict(index=index[i, :count[i]].copy(), r=r[i, :count[i], :3].astype(np.float64), dr=r[i, :count[i], 3].astype(np.float64),
                      min=mn[i, :count[i]].astype(bool), shift=sh[i, :count[i]].copy()) for i in range(n)]
+
+
+class MD:
+    """Velocity-Verlet MD with the engine's forces, state resident on the GPU (nnpgpu_md_*)."""
+
+    def __init__(self, eng, struc, mass, dt, skin=1.0, vel=None, flags=0):
+        self.eng = eng
+        self.n = struc.posn.shape[0]
+        posn = np.ascontiguousarray(struc.posn, dtype=np.float64)
+        species = np.ascontiguousarray(struc.species, dtype=np.int32)
+        mass = np.ascontiguousarray(np.broadcast_to(np.asarray(mass, dtype=np.float64), (self.n,)))
+        v = None if vel is None else np.ascontiguousarray(vel, dtype=np.float64)
+        h = ctypes.c_void_p()
+        eng._check(eng.lib.nnpgpu_md_create(eng._ctx, self.n, _p(posn), _p(v), _p(species), _p(mass), _p(_cell_colmajor(struc.cell)),
+                                            float(dt), float(skin), flags, ctypes.byref(h)))
+        self._h = h
+
+    def forces(self):
+        pe = np.zeros(1)
+        self.eng._check(self.eng.lib.nnpgpu_md_forces(self._h, _p(pe)))
+        return float(pe[0])
+
+    def run(self, nsteps):
+        pe, ke = np.zeros(nsteps), np.zeros(nsteps)
+        self.eng._check(self.eng.lib.nnpgpu_md_run(self._h, nsteps, _p(pe), _p(ke)))
+        return pe, ke
+
+    def state(self):
+        x, v, F = np.zeros((self.n, 3)), np.zeros((self.n, 3)), np.zeros((self.n, 3))
+        nb = ctypes.c_int()
+        self.eng._check(self.eng.lib.nnpgpu_md_state(self._h, _p(x), _p(v), _p(F), ctypes.byref(nb)))
+        return x, v, F, nb.value
+
+    def close(self):
+        if self._h:
+            self.eng.lib.nnpgpu_md_destroy(self._h)
+            self._h = None

@@ -153,6 +153,33 @@ int nnpgpu_submit(nnpgpu_ctx* ctx, int natoms, const double* posn, const int* sp
 int nnpgpu_poll(nnpgpu_ctx* ctx, long long request_id, double* energy, double* force, double* latency_s);
 int nnpgpu_serve_stop(nnpgpu_ctx* ctx);
 
+/* ---- molecular dynamics on resident device state.  Replaces the reference's MD job
+ * (src/torch/torch.cpp:267-275): velocity-Verlet steps (Verlet::compute,
+ * src/torch/integrator.cpp:170-193) around Engine::compute (src/torch/engine.cpp:107-118) with the
+ * NNP potential PotNNPE::compute (src/torch/pot_nnpe.cpp:175-295: energy including the species
+ * vacuum energies, forces with NNP::force's minimum-image rule).  Positions, velocities, forces
+ * and masses stay on the GPU.  Units as the reference: v += (dt/2) F/m with F in the potential's
+ * force unit and mass in whatever unit the caller pairs with dt (no conversion).  The first step
+ * starts from zero forces, as the reference's MD job does; call nnpgpu_md_forces first for a
+ * step that starts from the forces at the initial positions.
+ * Neighbour lists: a list at rc + skin stays resident and is refreshed exactly at rc every step
+ * (each step's forces equal a fresh list's), rebuilt when an atom has moved more than skin/2;
+ * skin = 0, or a cell with several images of an atom within rc, rebuilds every step.
+ *   posn, vel (may be NULL = zero) natoms*3; species natoms; mass natoms (per atom, > 0);
+ *   cell 9 (column-major lattice vectors); flags: NNPGPU_BF16 or 0. */
+typedef struct nnpgpu_md nnpgpu_md;
+int nnpgpu_md_create(nnpgpu_ctx* ctx, int natoms, const double* posn, const double* vel, const int* species,
+                     const double* mass, const double* cell, double dt, double skin, int flags, nnpgpu_md** out);
+/* forces and potential energy at the current positions (no step) */
+int nnpgpu_md_forces(nnpgpu_md* md, double* pe);
+/* nsteps velocity-Verlet steps; pe[t], ke[t] (may be NULL) receive each step's potential energy
+ * and kinetic energy 0.5 sum m |v|^2 */
+int nnpgpu_md_run(nnpgpu_md* md, int nsteps, double* pe, double* ke);
+/* positions (wrapped into the cell as Cell::returnToCell, src/struc/cell.cpp:84-94), velocities,
+ * forces (each may be NULL) and the number of resident-list builds so far */
+int nnpgpu_md_state(nnpgpu_md* md, double* posn, double* vel, double* force, int* rebuilds);
+void nnpgpu_md_destroy(nnpgpu_md* md);
+
 #ifdef __cplusplus
 }
 #endif
