@@ -14,6 +14,10 @@ constexpr int NE_MAX = 4;                          // distinct angular widths pe
 constexpr int NL = 2;                              // distinct lambda values per block
 constexpr int NZ_MAX = 6;                          // zeta = 2^m, m < NZ_MAX
 constexpr int NIN_MAX = 256;                       // network inputs
+constexpr int MOM_N = 4;                           // largest zeta of a moment-tensor block
+constexpr int MOM_C = 35;                          // symmetric tensor components of degree 0..MOM_N
+constexpr int MOM_Q = 20;                          // components of degree 0..MOM_N-1
+constexpr int MOM_EX = 8 * MOM_Q;                  // per-width floats a moment block needs in shared memory
 constexpr int NLAYER_MAX = 4;                      // network layers (hidden + output)
 constexpr int HID_MAX = 256;                       // nodes per layer
 
@@ -30,11 +34,13 @@ struct RadialP {
 // Angular basis of centre type I against neighbour pair block (J,K) (BasisA,
 // src/nnp/basis_angular.hpp:53-115), GAUSS form.  The block's functions are mapped onto a
 // grid (distinct 1/eta^alpha) x (distinct lambda) x (zeta = 2^m); gidx[f] is the grid cell
-// (e*NL + l)*NZ_MAX + m of file function f.
+// (e*NL + l)*NZ_MAX + m of file function f.  mom = 1 marks a block evaluated through moment
+// tensors (every zeta <= 4, |lambda| <= 1); its moments start at float moff of the atom's row.
 struct AngP {
   int n, off, cut, alpha;
   float rc, pirc, rci, norm;
-  int ne, nl, nz, pad;
+  int ne, nl, nz, mom;
+  int moff, pad0, pad1, pad2;
   float ietap[NE_MAX];
   float lam[NL];
   signed char gidx[NA_MAX];
@@ -44,6 +50,8 @@ struct PotParams {
   int ntypes;
   float rc;
   int nin[NT_MAX];
+  int mstride;  // floats of moment storage per atom (0: no moment blocks)
+  int pad[3];
   RadialP rad[NT_MAX][NT_MAX];
   AngP ang[NT_MAX][NB_MAX];
 };

@@ -40,6 +40,24 @@ struct SkinRef {
   int cap = 0;
 };
 
+// Geometry of one batch as uploaded to the device (per-structure metadata and atom offsets).
+struct Uploaded {
+  int natoms = 0, nstruc = 0, cap = 0, ncells = 0;
+  std::vector<StrucMeta> metas;
+  std::vector<int> offsets;
+};
+
+// The batch description behind the geometry currently on the device.
+struct MetaCache {
+  bool valid = false;
+  int generation = -1, cap = 0;
+  double rc = 0.0;
+  std::vector<int> natoms;
+  std::vector<double> cell;
+  std::vector<const void*> skins;  // per structure: j, code, cnt, cap
+  Uploaded U;
+};
+
 }  // namespace nnpgpu
 
 struct nnpgpu_ctx {
@@ -62,9 +80,10 @@ struct nnpgpu_ctx {
   nnpgpu::TuneCfg tune;
   // batch buffers
   nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, sfloor, nb_j, nb_r, nb_code, nb_cnt, nb_rev, orphans, G, dEdG, eatom, perm,
-      type_count, W, force, energy, status, cell_cnt, cell_start, cell_atoms, atom_cell;
+      type_count, W, force, energy, status, cell_cnt, cell_start, cell_atoms, atom_cell, mom;
   nnpgpu::HostBuf h_meta, h_in, h_out;  // pinned staging: geometry, inputs, outputs
   int buf_generation = 0;
+  nnpgpu::MetaCache meta_cache;
   // captured launch sequences of the batched path, keyed by batch shape
   typedef std::tuple<int, int, int, int, int, int, const void*, const void*, const void*, const void*> GraphKey;
   std::map<GraphKey, cudaGraphExec_t> graphs;

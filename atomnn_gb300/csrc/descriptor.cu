@@ -24,15 +24,19 @@ struct WarpSmem {
   int *orig, *toff;
 };
 
-__host__ __device__ inline size_t warp_smem_floats(int cap, int ne) { return (size_t)(12 + ne) * cap + 64 + 8; }
+// The per-width region ex is at least MOM_EX floats per width so that a moment block's tensors
+// (two sets of MOM_C per width plus the diagonal terms) fit there.
+__host__ __device__ inline int ex_stride(int cap) { return cap > MOM_EX ? cap : MOM_EX; }
+__host__ __device__ inline size_t warp_smem_floats(int cap, int ne) { return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + 64 + 8; }
 
 __device__ inline WarpSmem carve(float* base, int cap, int ne) {
   WarpSmem s;
   s.ux = base; s.uy = base + cap; s.uz = base + 2 * cap; s.d = base + 3 * cap; s.inv = base + 4 * cap;
   s.fc = base + 5 * cap; s.gc = base + 6 * cap; s.dpa = base + 7 * cap; s.ex = base + 8 * cap;
-  s.wx = base + (8 + ne) * cap; s.wy = base + (9 + ne) * cap; s.wz = base + (10 + ne) * cap;
-  s.orig = reinterpret_cast<int*>(base + (11 + ne) * cap);
-  s.scratch = base + (12 + ne) * cap;
+  float* w = s.ex + (size_t)ne * ex_stride(cap);
+  s.wx = w; s.wy = w + cap; s.wz = w + 2 * cap;
+  s.orig = reinterpret_cast<int*>(w + 3 * cap);
+  s.scratch = w + 4 * cap;
   s.toff = reinterpret_cast<int*>(s.scratch + 64);
   return s;
 }
@@ -41,6 +45,282 @@ __device__ __forceinline__ float powi(float x, int a) {
   float y = 1.f;
   for (int k = 0; k < a; ++k) y *= x;
   return y;
+}
+
+// ------------------------------------------------------------------------------- moment tensors
+// Blocks whose functions all have zeta <= 4 (and |lambda| <= 1) skip the triplet loop.  The
+// angular term ((1 + lambda cos)/2)^zeta is a polynomial of degree <= 4 in cos = u_j . u_k, and
+//   sum_{j in J, k in K} w_j w_k (u_j . u_k)^n = <M^J_n, M^K_n>,   M^S_n = sum_{j in S} w_j u_j^(x)n,
+// with w = exp(-r^alpha/eta^alpha) f_c(r) (the GAUSS pair factor, basis_angular.cpp:406-421).
+// The symmetric tensors M_n (n = 0..4) have 35 components in all, so a block costs
+// O(neighbours x 35) instead of O(neighbours^2); J == K blocks take half the full double sum
+// minus its j == k terms (the reference sums j < k, nnp.cpp:359-377).  The chain rule
+// differentiates each neighbour's term against the other species' moments, which the
+// descriptor pass leaves in global memory for the force pass.
+//
+// Component order: degree n ascending; within a degree, exponent a of u_x descending, then b of
+// u_y descending (c = n - a - b).
+__host__ __device__ constexpr int mom_off(int n) { return n * (n + 1) * (n + 2) / 6; }
+__host__ __device__ constexpr int mom_idx(int a, int b, int c) {
+  return mom_off(a + b + c) + (b + c) * (b + c + 1) / 2 + c;
+}
+__host__ __device__ constexpr float mom_fact(int n) {
+  float v = 1.0f;
+  for (int k = 2; k <= n; ++k) v *= (float)k;
+  return v;
+}
+// multinomial n!/(a! b! c!): the number of index tuples of the symmetric tensor per component
+__host__ __device__ constexpr float mom_mult(int a, int b, int c) {
+  return mom_fact(a + b + c) / (mom_fact(a) * mom_fact(b) * mom_fact(c));
+}
+__host__ __device__ constexpr int mom_deg(int r) { return r < 1 ? 0 : (r < 4 ? 1 : (r < 10 ? 2 : (r < 20 ? 3 : 4))); }
+
+// Moments of nsets slot ranges (set 0: [lo0,hi0), set 1: [lo1,hi1)) for every width of the block:
+// M[(set*ne + e)*MOM_C + r] = sum over the set's slots of w_e u^(a,b,c).  Each (set, width) pair
+// is summed by its own group of L lanes (L = 32 / pairs, rounded down to a power of two), so the
+// cross-lane reduction takes log2(L) shuffle levels instead of 5.  With Dg, set 0 also gives
+// Dg[e*(MOM_N+1) + n] = sum w_e^2 |u|^2n (the j == k terms of a J == K block).
+__device__ void build_moments(const WarpSmem& S, const AngP& A, int nsets, int lo0, int hi0, int lo1, int hi1, float* __restrict__ M,
+                              float* __restrict__ Dg) {
+  const int lane = threadIdx.x & 31;
+  const int pairs = nsets * A.ne;
+  int L = 32;
+  while (L * pairs > 32) L >>= 1;
+  const int grp = lane / L, sub = lane % L;
+  const bool active = grp < pairs;
+  const int set = active ? grp / A.ne : 0, e = active ? grp % A.ne : 0;
+  const int lo = active ? (set ? lo1 : lo0) : 0, hi = active ? (set ? hi1 : hi0) : 0;
+  const bool want_dg = Dg && set == 0;
+  float acc[MOM_C], dg[MOM_N + 1];
+#pragma unroll
+  for (int r = 0; r < MOM_C; ++r) acc[r] = 0.f;
+#pragma unroll
+  for (int n = 0; n <= MOM_N; ++n) dg[n] = 0.f;
+  const float ie = A.ietap[e];
+  for (int p = lo + sub; p < hi; p += L) {
+    const float d = S.d[p], ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
+    float f, g;
+    cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
+    const float w = expf(-ie * powi(d, A.alpha)) * f;
+    float wx[MOM_N + 1], py[MOM_N + 1], pz[MOM_N + 1];
+    wx[0] = w;
+    py[0] = 1.f;
+    pz[0] = 1.f;
+#pragma unroll
+    for (int k = 1; k <= MOM_N; ++k) {
+      wx[k] = wx[k - 1] * ux;
+      py[k] = py[k - 1] * uy;
+      pz[k] = pz[k - 1] * uz;
+    }
+#pragma unroll
+    for (int n = 0; n <= MOM_N; ++n)
+#pragma unroll
+      for (int a = n; a >= 0; --a)
+#pragma unroll
+        for (int b = n - a; b >= 0; --b) {
+          const int c = n - a - b;
+          acc[mom_idx(a, b, c)] = fmaf(wx[a], py[b] * pz[c], acc[mom_idx(a, b, c)]);
+        }
+    if (want_dg) {
+      const float u2 = ux * ux + uy * uy + uz * uz;
+      float t = w * w;
+#pragma unroll
+      for (int n = 0; n <= MOM_N; ++n) {
+        dg[n] += t;
+        t *= u2;
+      }
+    }
+  }
+  for (int o = L >> 1; o > 0; o >>= 1) {
+#pragma unroll
+    for (int r = 0; r < MOM_C; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+    if (Dg) {
+#pragma unroll
+      for (int n = 0; n <= MOM_N; ++n) dg[n] += __shfl_xor_sync(0xffffffffu, dg[n], o);
+    }
+  }
+  if (active && sub == 0) {
+#pragma unroll
+    for (int r = 0; r < MOM_C; ++r) M[(set * A.ne + e) * MOM_C + r] = acc[r];
+    if (want_dg) {
+#pragma unroll
+      for (int n = 0; n <= MOM_N; ++n) Dg[e * (MOM_N + 1) + n] = dg[n];
+    }
+  }
+}
+
+// coefficient of cos^n in ((1 + lam cos)/2)^zeta
+__device__ __forceinline__ float mom_coef(int zeta, float lam, int n) {
+  if (n > zeta) return 0.f;
+  float binom = 1.f, lp = 1.f;
+  for (int k = 0; k < n; ++k) {
+    binom = binom * (float)(zeta - k) / (float)(k + 1);
+    lp *= lam;
+  }
+  return ldexpf(binom * lp, -zeta);
+}
+
+// G4 of a moment block (BasisA::symm summed as in NNP::symm, nnp.cpp:359-377)
+__device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool same, int j0, int nJ, int k0, int nK, float* __restrict__ gmom,
+                               float* __restrict__ Gi, int cap) {
+  const int lane = threadIdx.x & 31;
+  const int nec = A.ne * MOM_C;
+  float* MJ = S.ex;
+  float* MK = same ? S.ex : S.ex + nec;
+  float* Dg = S.ex + 2 * nec;
+  build_moments(S, A, same ? 1 : 2, j0, j0 + nJ, k0, k0 + nK, MJ, same ? Dg : nullptr);
+  __syncwarp();
+  if (gmom) {
+    for (int t = lane; t < nec; t += 32) gmom[t] = MJ[t];
+    if (!same)
+      for (int t = lane; t < nec; t += 32) gmom[nec + t] = MK[t];
+  }
+  // V[e][n] = <M^J_n, M^K_n> (half the off-diagonal part for J == K)
+  float* V = S.scratch;
+  if (lane < A.ne * (MOM_N + 1)) {
+    const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
+    float s = 0.f;
+    for (int a = n; a >= 0; --a)
+      for (int b = n - a; b >= 0; --b) {
+        const int r = mom_idx(a, b, n - a - b);
+        s = fmaf(mom_mult(a, b, n - a - b) * MJ[e * MOM_C + r], MK[e * MOM_C + r], s);
+      }
+    if (same) s = 0.5f * (s - Dg[e * (MOM_N + 1) + n]);
+    V[lane] = s;
+  }
+  __syncwarp();
+  for (int f = lane; f < A.n; f += 32) {
+    const int cell = A.gidx[f];
+    const int e = cell / (NL * NZ_MAX), zeta = 1 << (cell % NZ_MAX);
+    const float lam = A.lam[(cell / NZ_MAX) % NL];
+    float v = 0.f;
+    for (int n = 0; n <= zeta; ++n) v = fmaf(mom_coef(zeta, lam, n), V[e * (MOM_N + 1) + n], v);
+    Gi[A.off + f] = A.norm * v;
+  }
+  __syncwarp();
+}
+
+// W_p -= d/dr_p of w_p(r) sum_n b_n <u_p^(x)n, B_n> for the slots [lo,hi).  With
+// S_n = <u^(x)n, B_n> and V_n = <u^(x)(n-1), B_n> (a vector) the gradient is
+// w' u sum_n b_n S_n + (w/r) sum_n n b_n (V_n - (u . V_n) u), and sum_n b_n S_n = b_0 B_0 + u . sum_n b_n V_n.
+// T3[e*MOM_Q + q] holds b_n times the three components of B_n one degree above component q
+// (n = deg q + 1), T0[e] = b_0 B_0; diag adds the j == k term of a J == K block.
+__device__ void mom_contract(const WarpSmem& S, const AngP& A, int lo, int hi, const float4* __restrict__ T3, const float* __restrict__ T0,
+                             const float* __restrict__ b, bool diag) {
+  const int lane = threadIdx.x & 31;
+  for (int p = lo + lane; p < hi; p += 32) {
+    const float d = S.d[p], ux = S.ux[p], uy = S.uy[p], uz = S.uz[p], inv = S.inv[p];
+    float f, g;
+    cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
+    const float da = powi(d, A.alpha);
+    const float dpa = (float)A.alpha * powi(d, A.alpha - 1) * f;
+    float px[MOM_N], pyz[MOM_N][MOM_N];
+    {
+      float py[MOM_N], pz[MOM_N];
+      px[0] = py[0] = pz[0] = 1.f;
+#pragma unroll
+      for (int k = 1; k < MOM_N; ++k) {
+        px[k] = px[k - 1] * ux;
+        py[k] = py[k - 1] * uy;
+        pz[k] = pz[k - 1] * uz;
+      }
+#pragma unroll
+      for (int bb = 0; bb < MOM_N; ++bb)
+#pragma unroll
+        for (int c = 0; bb + c < MOM_N; ++c) pyz[bb][c] = py[bb] * pz[c];
+    }
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    for (int e = 0; e < A.ne; ++e) {
+      const float x = expf(-A.ietap[e] * da);
+      const float w = x * f;
+      const float wd = x * (g - A.ietap[e] * dpa);
+      const float4* __restrict__ Te = T3 + e * MOM_Q;
+      float vx[MOM_N], vy[MOM_N], vz[MOM_N];  // b_n V_n per degree n = 1..MOM_N
+#pragma unroll
+      for (int n = 0; n < MOM_N; ++n) vx[n] = vy[n] = vz[n] = 0.f;
+#pragma unroll
+      for (int n = 1; n <= MOM_N; ++n)
+#pragma unroll
+        for (int a = n - 1; a >= 0; --a)
+#pragma unroll
+          for (int bb = n - 1 - a; bb >= 0; --bb) {
+            const int c = n - 1 - a - bb;
+            const float m = mom_mult(a, bb, c) * px[a] * pyz[bb][c];
+            const float4 t = Te[mom_idx(a, bb, c)];
+            vx[n - 1] = fmaf(m, t.x, vx[n - 1]);
+            vy[n - 1] = fmaf(m, t.y, vy[n - 1]);
+            vz[n - 1] = fmaf(m, t.z, vz[n - 1]);
+          }
+      float p1x = 0.f, p1y = 0.f, p1z = 0.f, p2x = 0.f, p2y = 0.f, p2z = 0.f;
+#pragma unroll
+      for (int n = 1; n <= MOM_N; ++n) {
+        p1x += vx[n - 1];
+        p1y += vy[n - 1];
+        p1z += vz[n - 1];
+        p2x = fmaf((float)n, vx[n - 1], p2x);
+        p2y = fmaf((float)n, vy[n - 1], p2y);
+        p2z = fmaf((float)n, vz[n - 1], p2z);
+      }
+      const float eb = T0[e] + ux * p1x + uy * p1y + uz * p1z;
+      const float up2 = ux * p2x + uy * p2y + uz * p2z;
+      const float s2 = w * inv;
+      float s1 = wd * eb - s2 * up2;
+      if (diag) {
+        float bs = 0.f;
+#pragma unroll
+        for (int n = 0; n <= MOM_N; ++n) bs += b[e * (MOM_N + 1) + n];
+        s1 -= w * wd * bs;
+      }
+      gx = fmaf(s1, ux, fmaf(s2, p2x, gx));
+      gy = fmaf(s1, uy, fmaf(s2, p2y, gy));
+      gz = fmaf(s1, uz, fmaf(s2, p2z, gz));
+    }
+    S.wx[p] -= gx;
+    S.wy[p] -= gy;
+    S.wz[p] -= gz;
+  }
+}
+
+// chain rule of a moment block (BasisA::force summed as in NNP::force, nnp.cpp:466-478)
+__device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool same, int j0, int nJ, int k0, int nK, const float* __restrict__ gmom,
+                                const float* __restrict__ gi) {
+  const int lane = threadIdx.x & 31;
+  const int nec = A.ne * MOM_C;
+  // b[e][n] = norm * sum over the block's functions of width e of dE/dG_f * coef_n(f)
+  float* b = S.scratch;
+  float* T0 = S.scratch + 32;  // [set][e]
+  if (lane < A.ne * (MOM_N + 1)) {
+    const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
+    float s = 0.f;
+    for (int f = 0; f < A.n; ++f) {
+      const int cell = A.gidx[f];
+      if (cell / (NL * NZ_MAX) != e) continue;
+      s = fmaf(gi[A.off + f], mom_coef(1 << (cell % NZ_MAX), A.lam[(cell / NZ_MAX) % NL], n), s);
+    }
+    b[lane] = A.norm * s;
+  }
+  __syncwarp();
+  // the contraction tables of each set: b_(deg q + 1) times the three components one degree up
+  float4* TJ = reinterpret_cast<float4*>(S.ex);
+  float4* TK = same ? TJ : TJ + A.ne * MOM_Q;
+  const int nsets = same ? 1 : 2;
+  for (int t = lane; t < nsets * A.ne * MOM_Q; t += 32) {
+    const int set = t / (A.ne * MOM_Q), e = (t / MOM_Q) % A.ne, q = t % MOM_Q;
+    // exponents of component q
+    int n = mom_deg(q), rem = q - mom_off(n), a = n, bc = 0;
+    while (rem > bc) { rem -= bc + 1; ++bc; --a; }
+    const int c = rem, bb = n - a - c;
+    const float bn = b[e * (MOM_N + 1) + n + 1];
+    const float* Mg = gmom + set * nec + e * MOM_C;
+    (set ? TK : TJ)[e * MOM_Q + q] =
+        make_float4(bn * Mg[mom_idx(a + 1, bb, c)], bn * Mg[mom_idx(a, bb + 1, c)], bn * Mg[mom_idx(a, bb, c + 1)], 0.f);
+  }
+  if (lane < nsets * A.ne) T0[lane] = b[(lane % A.ne) * (MOM_N + 1)] * gmom[(lane / A.ne) * nec + (lane % A.ne) * MOM_C];
+  __syncwarp();
+  // J's slots against the K moments (J's own for J == K); K's slots against the J moments
+  mom_contract(S, A, j0, j0 + nJ, TK, T0 + (same ? 0 : A.ne), b, same);
+  if (!same) mom_contract(S, A, k0, k0 + nK, TJ, T0, b, false);
+  __syncwarp();
 }
 
 // Stage the neighbour slots of atom i in shared memory, grouped by neighbour type.
@@ -349,7 +629,7 @@ template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                    const int* __restrict__ type, const int* __restrict__ nb_j,
                                                    const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt,
-                                                   float* __restrict__ G, int gstride) {
+                                                   float* __restrict__ G, int gstride, float* __restrict__ mom, int mstride) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
@@ -392,6 +672,10 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       if (A.n == 0) continue;
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
+      if (A.mom) {
+        symm_mom_block(S, A, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi, cap);
+        continue;
+      }
       block_pair_factors(S, A, j0, j0 + nJ, cap, true);
       if (K != J) block_pair_factors(S, A, k0, k0 + nK, cap, true);
       __syncwarp();
@@ -407,7 +691,8 @@ template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
                                                     const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt,
-                                                    const float* __restrict__ dEdG, int gstride, float4* __restrict__ W) {
+                                                    const float* __restrict__ dEdG, int gstride, const float* __restrict__ mom,
+                                                    int mstride, float4* __restrict__ W) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
@@ -450,6 +735,10 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
+      if (A.mom) {
+        force_mom_block(S, A, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
+        continue;
+      }
       block_pair_factors(S, A, j0, j0 + nJ, cap, false);
       if (K != J) block_pair_factors(S, A, k0, k0 + nK, cap, false);
       // dE/dG on the function grid (duplicates of a grid cell add up)
@@ -475,14 +764,14 @@ static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cuda
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   symm_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.G, B.gstride);
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
 }
 template <int NEK, int NZK>
 static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   force_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps), st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.W);
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
 }
 
 // Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).

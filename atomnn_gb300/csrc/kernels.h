@@ -39,6 +39,7 @@ struct BatchDev {
   // descriptors and networks
   float* G = nullptr;      // [natoms*gstride]
   float* dEdG = nullptr;   // [natoms*gstride]
+  float* mom = nullptr;    // [natoms*mstride] moment tensors of moment blocks (descriptor pass -> chain rule)
   int gstride = 0;
   float* eatom = nullptr;  // [natoms] network output
   int* perm = nullptr;     // [natoms] atoms grouped by type

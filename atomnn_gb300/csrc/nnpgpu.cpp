@@ -1,6 +1,7 @@
 // nnpgpu.cpp - the C ABI (include/nnpgpu.h): context, batch set-up and the launch sequence.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -247,16 +248,34 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
 // ------------------------------------------------------------------------------------------
 namespace {
 
-struct Uploaded {
-  int natoms = 0, nstruc = 0, cap = 0, ncells = 0;
-  std::vector<StrucMeta> metas;
-  std::vector<int> offsets;
-};
 
 // Validates the batch description and uploads geometry metadata; sizes all batch buffers.
+// True when the device already holds the geometry of exactly this batch description (same
+// cutoff, capacity, atom counts, cells, skin lists and buffers): repeated steps of one batch then
+// skip the per-structure set-up and its upload.
+static bool meta_cached(const nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, int cap, const SkinRef* skins) {
+  const MetaCache& m = c->meta_cache;
+  if (!m.valid || m.generation != c->buf_generation || m.rc != c->pot.rc || m.cap != cap || m.U.nstruc != nstruc) return false;
+  if (nstruc == 0) return true;
+  if (std::memcmp(m.natoms.data(), natoms, sizeof(int) * nstruc) != 0) return false;
+  if (std::memcmp(m.cell.data(), cell, sizeof(double) * 9 * nstruc) != 0) return false;
+  for (int s = 0; s < nstruc; ++s) {
+    const SkinRef r = skins ? skins[s] : SkinRef();
+    if (m.skins[4 * s] != r.j || m.skins[4 * s + 1] != r.code || m.skins[4 * s + 2] != r.cnt || m.skins[4 * s + 3] != (const void*)(intptr_t)r.cap)
+      return false;
+  }
+  return true;
+}
+
 int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, int cap, Uploaded& U, cudaStream_t st,
             const SkinRef* skins = nullptr) {
   if (nstruc < 0 || (nstruc > 0 && (!natoms || !cell))) return set_error(c, NNPGPU_ERR_INVALID, "invalid batch description");
+  if (meta_cached(c, nstruc, natoms, cell, cap, skins)) {
+    U = c->meta_cache.U;
+    cudaMemsetAsync(c->status.p, 0, sizeof(int) * ST_WORDS, st);
+    return NNPGPU_OK;
+  }
+  c->meta_cache.valid = false;
   U.nstruc = nstruc;
   U.offsets.assign(nstruc + 1, 0);
   for (int s = 0; s < nstruc; ++s) {
@@ -300,7 +319,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
        ensure(c, c->eatom, sizeof(float) * N) && ensure(c, c->perm, sizeof(int) * N) &&
        ensure(c, c->type_count, sizeof(int) * (3 * NT_MAX + 3)) && ensure(c, c->W, sizeof(float4) * NC) &&
        ensure(c, c->force, sizeof(double) * 3 * N) && ensure(c, c->energy, sizeof(double) * std::max(nstruc, 1)) &&
-       ensure(c, c->status, sizeof(int) * ST_WORDS);
+       ensure(c, c->status, sizeof(int) * ST_WORDS) && (c->P.mstride == 0 || ensure(c, c->mom, sizeof(float) * N * c->P.mstride));
   if (ok && U.ncells > 0) {
     // cell counts must start at zero: fresh memory is cleared, later calls leave them at zero
     const size_t before = c->cell_cnt.bytes;  // a grown buffer is a new allocation
@@ -324,6 +343,22 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
   cudaMemcpyAsync(c->imgs.p, h + meta_bytes, img_bytes, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->atom_struc.p, h + meta_bytes + img_bytes, as_bytes, cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(c->status.p, 0, sizeof(int) * ST_WORDS, st);
+  MetaCache& m = c->meta_cache;
+  m.valid = true;
+  m.generation = c->buf_generation;
+  m.rc = c->pot.rc;
+  m.cap = cap;
+  m.natoms.assign(natoms, natoms + nstruc);
+  m.cell.assign(cell, cell + 9 * (size_t)nstruc);
+  m.skins.resize(4 * (size_t)nstruc);
+  for (int s = 0; s < nstruc; ++s) {
+    const SkinRef r = skins ? skins[s] : SkinRef();
+    m.skins[4 * s] = r.j;
+    m.skins[4 * s + 1] = r.code;
+    m.skins[4 * s + 2] = r.cnt;
+    m.skins[4 * s + 3] = (const void*)(intptr_t)r.cap;
+  }
+  m.U = U;
   return NNPGPU_OK;
 }
 
@@ -357,6 +392,7 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.orphan_cap = std::max(U.natoms, 1);
   B.G = (float*)c->G.p;
   B.dEdG = (float*)c->dEdG.p;
+  B.mom = (float*)c->mom.p;
   B.gstride = c->gstride;
   B.eatom = (float*)c->eatom.p;
   B.perm = (int*)c->perm.p;
@@ -545,7 +581,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
-                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell};
+                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);

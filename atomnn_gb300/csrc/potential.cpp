@@ -213,7 +213,9 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
   P.rc = (float)pot.rc;
   ne_max = 1;
   nz_max = 1;
+  P.mstride = 0;
   for (int I = 0; I < pot.ntypes; ++I) {
+    int moff = 0;  // moment floats of this centre type so far
     if (pot.nin[I] > NIN_MAX) unsup("more than " + std::to_string(NIN_MAX) + " network inputs");
     P.nin[I] = pot.nin[I];
     for (int J = 0; J < pot.ntypes; ++J) {
@@ -276,9 +278,24 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
         a.gidx[f] = (signed char)((e * NL + l) * NZ_MAX + m);
       }
       a.nz = nz;
+      // zeta <= 4 with |lambda| <= 1: ((1 + lambda cos)/2)^zeta is a polynomial of degree <= 4
+      // in cos with a non-negative base, which the moment-tensor path evaluates
+      bool lam_ok = true;
+      for (int l = 0; l < a.nl; ++l) lam_ok = lam_ok && std::fabs((double)lams[l]) <= 1.0;
+      if ((1 << (nz - 1)) <= MOM_N && lam_ok) {
+        int J = 0, K = 0;
+        for (int x = 0; x < pot.ntypes; ++x)
+          for (int y = x; y < pot.ntypes; ++y)
+            if (lidx(x, y) == q) { J = x; K = y; }
+        a.mom = 1;
+        a.moff = moff;
+        moff += (J == K ? 1 : 2) * a.ne * MOM_C;
+      } else {
+        nz_max = std::max(nz_max, nz);  // the triplet kernels' zeta chain covers triplet blocks only
+      }
       ne_max = std::max(ne_max, a.ne);
-      nz_max = std::max(nz_max, nz);
     }
+    P.mstride = std::max(P.mstride, (moff + 3) / 4 * 4);
     const HNet& net = pot.nets[I];
     if (net.act <= 0) unsup("network activation not implemented on the GPU");
     if ((int)net.nodes.size() < 2 || (int)net.nodes.size() > NLAYER_MAX) unsup("networks need 1 to 3 hidden layers");
