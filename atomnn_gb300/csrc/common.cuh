@@ -52,6 +52,9 @@ struct PotParams {
   int nin[NT_MAX];
   int mstride;  // floats of moment storage per atom (0: no moment blocks)
   int pad[3];
+  // cutoff shared by every basis of centre type I (ccut 0: the bases differ)
+  int ccut[NT_MAX];
+  float crc[NT_MAX], cpirc[NT_MAX], crci[NT_MAX];
   RadialP rad[NT_MAX][NT_MAX];
   AngP ang[NT_MAX][NB_MAX];
 };
@@ -180,11 +183,11 @@ __device__ __forceinline__ void cutoff_fg(int cut, float d, float rc, float pirc
   if (cut == CUT_COS) {
     if (d < rc) {
       float s, c;
-      sincosf(d * pirc, &s, &c);
+      __sincosf(d * pirc, &s, &c);
       f = 0.5f * (c + 1.0f);
       g = -0.5f * pirc * s;
     } else {
-      f = (d > rc) ? 0.f : 0.5f * (cosf(d * pirc) + 1.0f);
+      f = (d > rc) ? 0.f : 0.5f * (__cosf(d * pirc) + 1.0f);
       g = 0.f;
     }
   } else if (cut == CUT_TANH) {

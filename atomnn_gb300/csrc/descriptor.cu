@@ -8,6 +8,9 @@
 // so the partner-side force contribution is a conflict-free shared-memory update, and the
 // owner-side one stays in registers; no atomics are used.
 //
+// Exponentials and the cosine cutoff use the hardware approximations (__expf, __sincosf: a few
+// ulp, below the FP32 rounding of the sums they enter).
+//
 // Angular functions (GAUSS, basis_angular.cpp:406-446,456-640) are evaluated on a grid of
 // (distinct eta) x (lambda) x (zeta = 2^m):  exp(-(r_ij^a + r_ik^a)/eta^a) factorises into
 // per-pair terms, ((1+lambda cos)/2)^(2^m) is a chain of squarings, and the force pass needs
@@ -74,14 +77,24 @@ __host__ __device__ constexpr float mom_mult(int a, int b, int c) {
   return mom_fact(a + b + c) / (mom_fact(a) * mom_fact(b) * mom_fact(c));
 }
 __host__ __device__ constexpr int mom_deg(int r) { return r < 1 ? 0 : (r < 4 ? 1 : (r < 10 ? 2 : (r < 20 ? 3 : 4))); }
+// mom_mult per component, and for each component q of degree <= 3 the components q + e_x,
+// q + e_y, q + e_z (runtime-indexed copies of the constexpr functions above)
+__device__ const float c_mom_mult[MOM_C] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 1, 1, 3, 3, 3, 6, 3, 1, 3,
+                                            3, 1, 1, 4, 4, 6, 12, 6, 4, 12, 12, 4, 1, 4, 6, 4, 1};
+__device__ const signed char c_mom_up[MOM_Q][3] = {{1, 2, 3},    {4, 5, 6},    {5, 7, 8},    {6, 8, 9},    {10, 11, 12},
+                                                   {11, 13, 14}, {12, 14, 15}, {13, 16, 17}, {14, 17, 18}, {15, 18, 19},
+                                                   {20, 21, 22}, {21, 23, 24}, {22, 24, 25}, {23, 26, 27}, {24, 27, 28},
+                                                   {25, 28, 29}, {26, 30, 31}, {27, 31, 32}, {28, 32, 33}, {29, 33, 34}};
+// binomial(zeta, n) for zeta = 1, 2, 4
+__device__ const float c_mom_binom[3][MOM_N + 1] = {{1, 1, 0, 0, 0}, {1, 2, 1, 0, 0}, {1, 4, 6, 4, 1}};
 
 // Moments of nsets slot ranges (set 0: [lo0,hi0), set 1: [lo1,hi1)) for every width of the block:
 // M[(set*ne + e)*MOM_C + r] = sum over the set's slots of w_e u^(a,b,c).  Each (set, width) pair
 // is summed by its own group of L lanes (L = 32 / pairs, rounded down to a power of two), so the
 // cross-lane reduction takes log2(L) shuffle levels instead of 5.  With Dg, set 0 also gives
 // Dg[e*(MOM_N+1) + n] = sum w_e^2 |u|^2n (the j == k terms of a J == K block).
-__device__ void build_moments(const WarpSmem& S, const AngP& A, int nsets, int lo0, int hi0, int lo1, int hi1, float* __restrict__ M,
-                              float* __restrict__ Dg) {
+__device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nsets, int lo0, int hi0, int lo1, int hi1,
+                              float* __restrict__ M, float* __restrict__ Dg) {
   const int lane = threadIdx.x & 31;
   const int pairs = nsets * A.ne;
   int L = 32;
@@ -100,8 +113,9 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, int nsets, int l
   for (int p = lo + sub; p < hi; p += L) {
     const float d = S.d[p], ux = S.ux[p], uy = S.uy[p], uz = S.uz[p];
     float f, g;
-    cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
-    const float w = expf(-ie * powi(d, A.alpha)) * f;
+    if (cc) f = S.fc[p];
+    else cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
+    const float w = __expf(-ie * powi(d, A.alpha)) * f;
     float wx[MOM_N + 1], py[MOM_N + 1], pz[MOM_N + 1];
     wx[0] = w;
     py[0] = 1.f;
@@ -149,26 +163,22 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, int nsets, int l
   }
 }
 
-// coefficient of cos^n in ((1 + lam cos)/2)^zeta
-__device__ __forceinline__ float mom_coef(int zeta, float lam, int n) {
-  if (n > zeta) return 0.f;
-  float binom = 1.f, lp = 1.f;
-  for (int k = 0; k < n; ++k) {
-    binom = binom * (float)(zeta - k) / (float)(k + 1);
-    lp *= lam;
-  }
-  return ldexpf(binom * lp, -zeta);
+// coefficient of cos^n in ((1 + lam cos)/2)^zeta, zeta = 2^m <= 4
+__device__ __forceinline__ float mom_coef(int m, float lam, int n) {
+  float lp = 1.f;
+  for (int k = 0; k < n; ++k) lp *= lam;
+  return c_mom_binom[m][n] * lp * (1.0f / (float)(1 << (1 << m)));
 }
 
 // G4 of a moment block (BasisA::symm summed as in NNP::symm, nnp.cpp:359-377)
-__device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool same, int j0, int nJ, int k0, int nK, float* __restrict__ gmom,
-                               float* __restrict__ Gi, int cap) {
+__device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool same, int j0, int nJ, int k0, int nK, float* __restrict__ gmom,
+                               float* __restrict__ Gi) {
   const int lane = threadIdx.x & 31;
   const int nec = A.ne * MOM_C;
   float* MJ = S.ex;
   float* MK = same ? S.ex : S.ex + nec;
   float* Dg = S.ex + 2 * nec;
-  build_moments(S, A, same ? 1 : 2, j0, j0 + nJ, k0, k0 + nK, MJ, same ? Dg : nullptr);
+  build_moments(S, A, cc, same ? 1 : 2, j0, j0 + nJ, k0, k0 + nK, MJ, same ? Dg : nullptr);
   __syncwarp();
   if (gmom) {
     for (int t = lane; t < nec; t += 32) gmom[t] = MJ[t];
@@ -180,22 +190,21 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool same, int 
   if (lane < A.ne * (MOM_N + 1)) {
     const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
     float s = 0.f;
-    for (int a = n; a >= 0; --a)
-      for (int b = n - a; b >= 0; --b) {
-        const int r = mom_idx(a, b, n - a - b);
-        s = fmaf(mom_mult(a, b, n - a - b) * MJ[e * MOM_C + r], MK[e * MOM_C + r], s);
-      }
+    for (int r = mom_off(n); r < mom_off(n + 1); ++r) s = fmaf(c_mom_mult[r] * MJ[e * MOM_C + r], MK[e * MOM_C + r], s);
     if (same) s = 0.5f * (s - Dg[e * (MOM_N + 1) + n]);
     V[lane] = s;
   }
   __syncwarp();
   for (int f = lane; f < A.n; f += 32) {
     const int cell = A.gidx[f];
-    const int e = cell / (NL * NZ_MAX), zeta = 1 << (cell % NZ_MAX);
+    const int e = cell / (NL * NZ_MAX), m = cell % NZ_MAX, zeta = 1 << m;
     const float lam = A.lam[(cell / NZ_MAX) % NL];
-    float v = 0.f;
-    for (int n = 0; n <= zeta; ++n) v = fmaf(mom_coef(zeta, lam, n), V[e * (MOM_N + 1) + n], v);
-    Gi[A.off + f] = A.norm * v;
+    float v = 0.f, lp = 1.f;
+    for (int n = 0; n <= zeta; ++n) {
+      v = fmaf(c_mom_binom[m][n] * lp, V[e * (MOM_N + 1) + n], v);
+      lp *= lam;
+    }
+    Gi[A.off + f] = A.norm * v * (1.0f / (float)(1 << zeta));
   }
   __syncwarp();
 }
@@ -205,13 +214,18 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool same, int 
 // w' u sum_n b_n S_n + (w/r) sum_n n b_n (V_n - (u . V_n) u), and sum_n b_n S_n = b_0 B_0 + u . sum_n b_n V_n.
 // T3[e*MOM_Q + q] holds b_n times the three components of B_n one degree above component q
 // (n = deg q + 1), T0[e] = b_0 B_0; diag adds the j == k term of a J == K block.
-__device__ void mom_contract(const WarpSmem& S, const AngP& A, int lo, int hi, const float4* __restrict__ T3, const float* __restrict__ T0,
-                             const float* __restrict__ b, bool diag) {
+__device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, int hi, const float4* __restrict__ T3,
+                             const float* __restrict__ T0, const float* __restrict__ b, bool diag) {
   const int lane = threadIdx.x & 31;
   for (int p = lo + lane; p < hi; p += 32) {
     const float d = S.d[p], ux = S.ux[p], uy = S.uy[p], uz = S.uz[p], inv = S.inv[p];
     float f, g;
-    cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
+    if (cc) {
+      f = S.fc[p];
+      g = S.gc[p];
+    } else {
+      cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
+    }
     const float da = powi(d, A.alpha);
     const float dpa = (float)A.alpha * powi(d, A.alpha - 1) * f;
     float px[MOM_N], pyz[MOM_N][MOM_N];
@@ -231,7 +245,7 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, int lo, int hi, c
     }
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int e = 0; e < A.ne; ++e) {
-      const float x = expf(-A.ietap[e] * da);
+      const float x = __expf(-A.ietap[e] * da);
       const float w = x * f;
       const float wd = x * (g - A.ietap[e] * dpa);
       const float4* __restrict__ Te = T3 + e * MOM_Q;
@@ -282,8 +296,8 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, int lo, int hi, c
 }
 
 // chain rule of a moment block (BasisA::force summed as in NNP::force, nnp.cpp:466-478)
-__device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool same, int j0, int nJ, int k0, int nK, const float* __restrict__ gmom,
-                                const float* __restrict__ gi) {
+__device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool same, int j0, int nJ, int k0, int nK,
+                                const float* __restrict__ gmom, const float* __restrict__ gi) {
   const int lane = threadIdx.x & 31;
   const int nec = A.ne * MOM_C;
   // b[e][n] = norm * sum over the block's functions of width e of dE/dG_f * coef_n(f)
@@ -295,7 +309,7 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool same, int
     for (int f = 0; f < A.n; ++f) {
       const int cell = A.gidx[f];
       if (cell / (NL * NZ_MAX) != e) continue;
-      s = fmaf(gi[A.off + f], mom_coef(1 << (cell % NZ_MAX), A.lam[(cell / NZ_MAX) % NL], n), s);
+      if (n <= (1 << (cell % NZ_MAX))) s = fmaf(gi[A.off + f], mom_coef(cell % NZ_MAX, A.lam[(cell / NZ_MAX) % NL], n), s);
     }
     b[lane] = A.norm * s;
   }
@@ -306,20 +320,15 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool same, int
   const int nsets = same ? 1 : 2;
   for (int t = lane; t < nsets * A.ne * MOM_Q; t += 32) {
     const int set = t / (A.ne * MOM_Q), e = (t / MOM_Q) % A.ne, q = t % MOM_Q;
-    // exponents of component q
-    int n = mom_deg(q), rem = q - mom_off(n), a = n, bc = 0;
-    while (rem > bc) { rem -= bc + 1; ++bc; --a; }
-    const int c = rem, bb = n - a - c;
-    const float bn = b[e * (MOM_N + 1) + n + 1];
+    const float bn = b[e * (MOM_N + 1) + mom_deg(q) + 1];
     const float* Mg = gmom + set * nec + e * MOM_C;
-    (set ? TK : TJ)[e * MOM_Q + q] =
-        make_float4(bn * Mg[mom_idx(a + 1, bb, c)], bn * Mg[mom_idx(a, bb + 1, c)], bn * Mg[mom_idx(a, bb, c + 1)], 0.f);
+    (set ? TK : TJ)[e * MOM_Q + q] = make_float4(bn * Mg[c_mom_up[q][0]], bn * Mg[c_mom_up[q][1]], bn * Mg[c_mom_up[q][2]], 0.f);
   }
   if (lane < nsets * A.ne) T0[lane] = b[(lane % A.ne) * (MOM_N + 1)] * gmom[(lane / A.ne) * nec + (lane % A.ne) * MOM_C];
   __syncwarp();
   // J's slots against the K moments (J's own for J == K); K's slots against the J moments
-  mom_contract(S, A, j0, j0 + nJ, TK, T0 + (same ? 0 : A.ne), b, same);
-  if (!same) mom_contract(S, A, k0, k0 + nK, TJ, T0, b, false);
+  mom_contract(S, A, cc, j0, j0 + nJ, TK, T0 + (same ? 0 : A.ne), b, same);
+  if (!same) mom_contract(S, A, cc, k0, k0 + nK, TJ, T0, b, false);
   __syncwarp();
 }
 
@@ -330,14 +339,20 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const int n = min(nb_cnt[i], cap);
+  // neighbour types, one chunk of 32 slots per register (cap <= 32 * QMAX)
+  int tq[QMAX];
   int cnt[NT_MAX];
 #pragma unroll
   for (int t = 0; t < NT_MAX; ++t) cnt[t] = 0;
-  for (int c = 0; c < n; c += 32) {
-    const int s = c + lane;
-    const int t = (s < n) ? clamp_type(type[nb_j[(size_t)i * cap + s]], ntypes) : -1;
 #pragma unroll
-    for (int tt = 0; tt < NT_MAX; ++tt) cnt[tt] += __popc(__ballot_sync(0xffffffffu, t == tt));
+  for (int q = 0; q < QMAX; ++q) {
+    const int s = q * 32 + lane;
+    tq[q] = -1;
+    if (q * 32 < n) {
+      tq[q] = (s < n) ? clamp_type(type[nb_j[(size_t)i * cap + s]], ntypes) : -1;
+#pragma unroll
+      for (int tt = 0; tt < NT_MAX; ++tt) cnt[tt] += __popc(__ballot_sync(0xffffffffu, tq[q] == tt));
+    }
   }
   int run[NT_MAX];
   int acc = 0;
@@ -348,10 +363,12 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
     acc += (t < ntypes) ? cnt[t] : 0;
   }
   if (lane == 0) S.toff[NT_MAX] = acc;
-  for (int c = 0; c < n; c += 32) {
-    const int s = c + lane;
+#pragma unroll
+  for (int q = 0; q < QMAX; ++q) {
+    if (q * 32 >= n) break;
+    const int s = q * 32 + lane;
     const size_t g = (size_t)i * cap + s;
-    const int t = (s < n) ? clamp_type(type[nb_j[g]], ntypes) : -1;
+    const int t = tq[q];
     int pos = 0;
 #pragma unroll
     for (int tt = 0; tt < NT_MAX; ++tt) {
@@ -384,7 +401,7 @@ __device__ void block_pair_factors(const WarpSmem& S, const AngP& A, int lo, int
     cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
     const float da = powi(d, A.alpha);
     for (int e = 0; e < A.ne; ++e) {
-      const float x = expf(-A.ietap[e] * da);
+      const float x = __expf(-A.ietap[e] * da);
       S.ex[e * cap + p] = with_fc ? x * f : x;
     }
     S.fc[p] = f;
@@ -624,6 +641,21 @@ __device__ void run_block(const WarpSmem& S, const AngP& A, const Sched& sc, int
 #undef NNP_CASE
 }
 
+// When every basis of centre type I shares one cutoff function and radius, evaluate it once per
+// staged neighbour (value and derivative into S.fc / S.gc) for all blocks to read.
+__device__ __forceinline__ bool cutoff_cache(const WarpSmem& S, const PotParams& P, int I, int n) {
+  if (!P.ccut[I]) return false;
+  const int lane = threadIdx.x & 31;
+  for (int p = lane; p < n; p += 32) {
+    float f, g;
+    cutoff_fg(P.ccut[I], S.d[p], P.crc[I], P.cpirc[I], P.crci[I], f, g);
+    S.fc[p] = f;
+    S.gc[p] = g;
+  }
+  __syncwarp();
+  return true;
+}
+
 // ------------------------------------------------------------------------------------ symm
 template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
@@ -636,33 +668,42 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
   if (i >= a0 + natoms) return;
   const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
   const int I = clamp_type(type[i], P.ntypes);
-  stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
+  const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
+  const bool cc = cutoff_cache(S, P, I, n);
   float* Gi = G + (size_t)i * gstride;
   for (int k = P.nin[I] + lane; k < gstride; k += 32) Gi[k] = 0.f;
 
-  // ---- radial: G2 of neighbour type J (BasisR::symm, basis_radial.cpp:302-310)
+  // ---- radial: G2 of neighbour type J (BasisR::symm, basis_radial.cpp:302-310); functions in
+  // groups of four, lanes over the type's neighbours
   for (int J = 0; J < P.ntypes; ++J) {
     const RadialP& R = P.rad[I][J];
-    float acc[NR_MAX];
+    const int p0 = S.toff[J], p1 = S.toff[J + 1];
+    for (int f0 = 0; f0 < R.n; f0 += 4) {
+      float rs[4], eta[4], acc[4];
 #pragma unroll
-    for (int f = 0; f < NR_MAX; ++f) acc[f] = 0.f;
-    for (int p = S.toff[J] + lane; p < S.toff[J + 1]; p += 32) {
-      const float d = S.d[p];
-      float fc, gc;
-      cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
-#pragma unroll
-      for (int f = 0; f < NR_MAX; ++f)
-        if (f < R.n) {
-          const float x = d - R.rs[f];
-          acc[f] += expf(-R.eta[f] * x * x) * fc;
-        }
-    }
-#pragma unroll
-    for (int f = 0; f < NR_MAX; ++f)
-      if (f < R.n) {
-        const float v = warp_sum(acc[f]);
-        if (lane == f) Gi[R.off + f] = v * R.norm;
+      for (int k = 0; k < 4; ++k) {
+        const bool on = f0 + k < R.n;
+        rs[k] = on ? R.rs[f0 + k] : 0.f;
+        eta[k] = on ? R.eta[f0 + k] : 0.f;
+        acc[k] = 0.f;
       }
+      for (int p = p0 + lane; p < p1; p += 32) {
+        const float d = S.d[p];
+        float fc, gc;
+        if (cc) fc = S.fc[p];
+        else cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const float x = d - rs[k];
+          acc[k] = fmaf(__expf(-eta[k] * x * x), fc, acc[k]);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float v = warp_sum(acc[k]);
+        if (lane == 0 && f0 + k < R.n) Gi[R.off + f0 + k] = v * R.norm;
+      }
+    }
   }
 
   // ---- angular blocks (J <= K): G4
@@ -673,7 +714,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (A.mom) {
-        symm_mom_block(S, A, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi, cap);
+        symm_mom_block(S, A, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
         continue;
       }
       block_pair_factors(S, A, j0, j0 + nJ, cap, true);
@@ -700,25 +741,28 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
   const int I = clamp_type(type[i], P.ntypes);
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
+  const bool cc = cutoff_cache(S, P, I, n);
   const float* gi = dEdG + (size_t)i * gstride;
 
   // ---- radial chain rule: W_p = BasisR::force(d) * u_p (basis_radial.cpp:371-380, nnp.cpp:441-446)
   for (int J = 0; J < P.ntypes; ++J) {
     const RadialP& R = P.rad[I][J];
-    float s[NR_MAX];
-#pragma unroll
-    for (int f = 0; f < NR_MAX; ++f) s[f] = (f < R.n) ? gi[R.off + f] : 0.f;
+    const float* __restrict__ sJ = gi + R.off;
     for (int p = S.toff[J] + lane; p < S.toff[J + 1]; p += 32) {
       const float d = S.d[p];
       float fc, gc;
-      cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
+      if (cc) {
+        fc = S.fc[p];
+        gc = S.gc[p];
+      } else {
+        cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
+      }
       float amp = 0.f;
-#pragma unroll
-      for (int f = 0; f < NR_MAX; ++f)
-        if (f < R.n) {
-          const float x = d - R.rs[f];
-          amp -= s[f] * expf(-R.eta[f] * x * x) * (-2.0f * R.eta[f] * x * fc + gc);
-        }
+#pragma unroll 1
+      for (int f = 0; f < R.n; ++f) {
+        const float x = d - R.rs[f], eta = R.eta[f];
+        amp -= sJ[f] * __expf(-eta * x * x) * (-2.0f * eta * x * fc + gc);
+      }
       amp *= R.norm;
       S.wx[p] = amp * S.ux[p];
       S.wy[p] = amp * S.uy[p];
@@ -736,7 +780,7 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
       if (A.mom) {
-        force_mom_block(S, A, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
+        force_mom_block(S, A, cc, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
         continue;
       }
       block_pair_factors(S, A, j0, j0 + nJ, cap, false);

@@ -296,6 +296,25 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
       ne_max = std::max(ne_max, a.ne);
     }
     P.mstride = std::max(P.mstride, (moff + 3) / 4 * 4);
+    // one cutoff function and radius for every basis of this centre type: the kernels then
+    // evaluate it once per neighbour
+    {
+      int cut = 0;
+      double rcv = 0.0;
+      bool same = true, any = false;
+      auto see = [&](int c, double r) {
+        if (!any) { cut = c; rcv = r; any = true; }
+        else if (c != cut || r != rcv) same = false;
+      };
+      for (int J = 0; J < pot.ntypes; ++J)
+        if (!pot.rad[I][J].rs.empty()) see(pot.rad[I][J].cut, pot.rad[I][J].rc);
+      for (int q = 0; q < pot.ntypes * (pot.ntypes + 1) / 2; ++q)
+        if (!pot.ang[I][q].eta.empty()) see(pot.ang[I][q].cut, pot.ang[I][q].rc);
+      P.ccut[I] = (same && any) ? cut : 0;
+      P.crc[I] = (float)rcv;
+      P.cpirc[I] = any ? (float)(kPi / rcv) : 0.f;
+      P.crci[I] = any ? (float)(1.0 / rcv) : 0.f;
+    }
     const HNet& net = pot.nets[I];
     if (net.act <= 0) unsup("network activation not implemented on the GPU");
     if ((int)net.nodes.size() < 2 || (int)net.nodes.size() > NLAYER_MAX) unsup("networks need 1 to 3 hidden layers");
