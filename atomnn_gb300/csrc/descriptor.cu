@@ -228,9 +228,10 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
     }
     const float da = powi(d, A.alpha);
     const float dpa = (float)A.alpha * powi(d, A.alpha - 1) * f;
-    float px[MOM_N], pyz[MOM_N][MOM_N];
+    // mult(q) u^(a,b,c) for the components q of degree <= 3, shared by every width
+    float mono[MOM_Q];
     {
-      float py[MOM_N], pz[MOM_N];
+      float px[MOM_N], py[MOM_N], pz[MOM_N];
       px[0] = py[0] = pz[0] = 1.f;
 #pragma unroll
       for (int k = 1; k < MOM_N; ++k) {
@@ -239,9 +240,14 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
         pz[k] = pz[k - 1] * uz;
       }
 #pragma unroll
-      for (int bb = 0; bb < MOM_N; ++bb)
+      for (int n = 0; n < MOM_N; ++n)
 #pragma unroll
-        for (int c = 0; bb + c < MOM_N; ++c) pyz[bb][c] = py[bb] * pz[c];
+        for (int a = n; a >= 0; --a)
+#pragma unroll
+          for (int bb = n - a; bb >= 0; --bb) {
+            const int c = n - a - bb;
+            mono[mom_idx(a, bb, c)] = mom_mult(a, bb, c) * px[a] * (py[bb] * pz[c]);
+          }
     }
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int e = 0; e < A.ne; ++e) {
@@ -259,7 +265,7 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
 #pragma unroll
           for (int bb = n - 1 - a; bb >= 0; --bb) {
             const int c = n - 1 - a - bb;
-            const float m = mom_mult(a, bb, c) * px[a] * pyz[bb][c];
+            const float m = mono[mom_idx(a, bb, c)];
             const float4 t = Te[mom_idx(a, bb, c)];
             vx[n - 1] = fmaf(m, t.x, vx[n - 1]);
             vy[n - 1] = fmaf(m, t.y, vy[n - 1]);
@@ -335,7 +341,8 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool 
 // Stage the neighbour slots of atom i in shared memory, grouped by neighbour type.
 // Returns the number of staged slots; toff[t]..toff[t+1] is the range of type t.
 __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, const int* __restrict__ type,
-                               const int* __restrict__ nb_j, const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt) {
+                               const int* __restrict__ nb_j, const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
+                               const int* __restrict__ nb_cnt) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const int n = min(nb_cnt[i], cap);
@@ -349,7 +356,8 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
     const int s = q * 32 + lane;
     tq[q] = -1;
     if (q * 32 < n) {
-      tq[q] = (s < n) ? clamp_type(type[nb_j[(size_t)i * cap + s]], ntypes) : -1;
+      const size_t g = (size_t)i * cap + s;
+      tq[q] = (s < n) ? clamp_type(nb_t ? (int)nb_t[g] : type[nb_j[g]], ntypes) : -1;
 #pragma unroll
       for (int tt = 0; tt < NT_MAX; ++tt) cnt[tt] += __popc(__ballot_sync(0xffffffffu, tq[q] == tt));
     }
@@ -660,15 +668,16 @@ __device__ __forceinline__ bool cutoff_cache(const WarpSmem& S, const PotParams&
 template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                    const int* __restrict__ type, const int* __restrict__ nb_j,
-                                                   const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt,
-                                                   float* __restrict__ G, int gstride, float* __restrict__ mom, int mstride) {
+                                                   const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
+                                                   const int* __restrict__ nb_cnt, float* __restrict__ G, int gstride,
+                                                   float* __restrict__ mom, int mstride) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
   const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
   const int I = clamp_type(type[i], P.ntypes);
-  const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
+  const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
   const bool cc = cutoff_cache(S, P, I, n);
   float* Gi = G + (size_t)i * gstride;
   for (int k = P.nin[I] + lane; k < gstride; k += 32) Gi[k] = 0.f;
@@ -731,16 +740,16 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
 template <int NEK, int NZK>
 __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
-                                                    const float4* __restrict__ nb_r, const int* __restrict__ nb_cnt,
-                                                    const float* __restrict__ dEdG, int gstride, const float* __restrict__ mom,
-                                                    int mstride, float4* __restrict__ W) {
+                                                    const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
+                                                    const int* __restrict__ nb_cnt, const float* __restrict__ dEdG, int gstride,
+                                                    const float* __restrict__ mom, int mstride, float4* __restrict__ W) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
   const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
   const int I = clamp_type(type[i], P.ntypes);
-  const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_r, nb_cnt);
+  const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
   const bool cc = cutoff_cache(S, P, I, n);
   const float* gi = dEdG + (size_t)i * gstride;
 
@@ -808,14 +817,14 @@ static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cuda
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   symm_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
 }
 template <int NEK, int NZK>
 static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   force_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps), st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
 }
 
 // Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).

@@ -26,6 +26,7 @@ struct BatchDev {
   int* nb_j = nullptr;
   float4* nb_r = nullptr;
   int* nb_code = nullptr;
+  unsigned char* nb_t = nullptr;  // species of each slot's neighbour (null: looked up from type[])
   int* nb_cnt = nullptr;
   int* nb_rev = nullptr;
   // cell lists of the structures in neighbour mode 4 (ncells entries, sentinels included)

@@ -48,6 +48,7 @@ __global__ void frac_kernel(int a0, int natoms, int ntypes, const int* __restric
   }  else {
     s = make_float4((float)p0, (float)p1, (float)p2, 0.f);
   }
+  s.w = __int_as_float(type ? clamp_type(type[i], ntypes) : 0);  // the species rides along for the lists
   sfrac[i] = s;
   sfloor[i] = fl;
   if (S.mode == 4) {
@@ -121,11 +122,13 @@ __global__ void cell_fill_kernel(int a0, int natoms, const int* __restrict__ ato
 }
 
 __device__ __forceinline__ void emit(int slot, int cap, int j, float rx, float ry, float rz, float dr, int code,
-                                     int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code) {
+                                     int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
+                                     unsigned char* __restrict__ nb_t, const float4* __restrict__ sfrac) {
   if (slot < cap) {
     nb_j[slot] = j;
     nb_r[slot] = make_float4(rx, ry, rz, dr);
     nb_code[slot] = code;
+    if (nb_t) nb_t[slot] = (unsigned char)__float_as_int(sfrac[j].w);
   }
 }
 
@@ -220,7 +223,8 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
                                                        const ImgEntry* __restrict__ imgs, const int* __restrict__ atom_cell,
                                                        const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
                                                        int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
-                                                       int* __restrict__ nb_cnt, int* __restrict__ status) {
+                                                       unsigned char* __restrict__ nb_t, int* __restrict__ nb_cnt,
+                                                       int* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
@@ -232,6 +236,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
   int* const oj = nb_j + (size_t)i * cap;
   float4* const orr = nb_r + (size_t)i * cap;
   int* const oc = nb_code + (size_t)i * cap;
+  unsigned char* const ot = nb_t ? nb_t + (size_t)i * cap : nullptr;
   const unsigned lt = (1u << lane) - 1u;
   int count = 0;  // warp-uniform
 
@@ -247,7 +252,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       int D[3] = {0, 0, 0};
       if (jl < nj && j != i) keep = single_image(S, si, fi, j, sfrac, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
-      if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc);
+      if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc, ot, sfrac);
       count += __popc(mk);
     }
   } else if (S.mode == 4) {
@@ -336,7 +341,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       const int slot = count + __popc(mk & lt);
       if (keep && slot < cap) {
-        st_j[slot] = j;
+        st_j[slot] = j | (__float_as_int(sfrac[j].w) << 30);  // species in the top two bits
         st_r[slot] = make_float4(r0, r1, r2, dr);
         st_c[slot] = pack_code(D[0], D[1], D[2], true);
       }
@@ -350,7 +355,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       for (int t = 0; t < NB_MASK_WORDS / 32; ++t) msk[lane + 32 * t] = 0u;
       __syncwarp();
       for (int e = lane; e < n; e += 32) {
-        const int jl = st_j[e] - j0;
+        const int jl = (st_j[e] & 0x3fffffff) - j0;
         atomicOr(&msk[jl >> 5], 1u << (jl & 31));
       }
       __syncwarp();
@@ -374,18 +379,20 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       }
       __syncwarp();
       for (int e = lane; e < n; e += 32) {
-        const int jg = st_j[e], jl = jg - j0;
+        const int jg = st_j[e] & 0x3fffffff, jl = jg - j0;
         const int rank = wpre[jl >> 5] + __popc(msk[jl >> 5] & ((1u << (jl & 31)) - 1u));
         oj[rank] = jg;
+        if (ot) ot[rank] = (unsigned char)((unsigned)st_j[e] >> 30);
         orr[rank] = st_r[e];
         oc[rank] = st_c[e];
       }
     } else {
       for (int e = lane; e < n; e += 32) {
-        const int jg = st_j[e];
+        const int jg = st_j[e] & 0x3fffffff;
         int rank = 0;
-        for (int f = 0; f < n; ++f) rank += (st_j[f] < jg) ? 1 : 0;
+        for (int f = 0; f < n; ++f) rank += ((st_j[f] & 0x3fffffff) < jg) ? 1 : 0;
         oj[rank] = jg;
+        if (ot) ot[rank] = (unsigned char)((unsigned)st_j[e] >> 30);
         orr[rank] = st_r[e];
         oc[rank] = st_c[e];
       }
@@ -435,7 +442,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
         }
       }
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
-      if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(T[0], T[1], T[2], true), oj, orr, oc);
+      if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(T[0], T[1], T[2], true), oj, orr, oc, ot, sfrac);
       count += __popc(mk);
     }
   } else if (S.mode == 1) {
@@ -518,7 +525,8 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
             dr = sqrtf(d2);
           }
           if (keep) {
-            emit(slot, cap, j, t0, t1, t2, dr, pack_code(D[0] + im[n].n[0], D[1] + im[n].n[1], D[2] + im[n].n[2], n == best), oj, orr, oc);
+            emit(slot, cap, j, t0, t1, t2, dr, pack_code(D[0] + im[n].n[0], D[1] + im[n].n[1], D[2] + im[n].n[2], n == best), oj, orr, oc,
+                 ot, sfrac);
             ++slot;
           }
         }
@@ -547,7 +555,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
         }
       }
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
-      if (keep) emit(count + __popc(mk & lt), cap, j0 + jl, r0, r1, r2, dr, pack_code(0, 0, 0, false), oj, orr, oc);
+      if (keep) emit(count + __popc(mk & lt), cap, j0 + jl, r0, r1, r2, dr, pack_code(0, 0, 0, false), oj, orr, oc, ot, sfrac);
       count += __popc(mk);
     }
   }
@@ -610,7 +618,7 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   }
   const int blocks = (B.natoms + warps - 1) / warps;
   neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
-                                             B.atom_cell, B.cell_start, B.cell_atoms, B.nb_j, B.nb_r, B.nb_code, B.nb_cnt, B.status);
+                                             B.atom_cell, B.cell_start, B.cell_atoms, B.nb_j, B.nb_r, B.nb_code, B.nb_t, B.nb_cnt, B.status);
 }
 
 void launch_reverse(const BatchDev& B, cudaStream_t st) {

@@ -314,6 +314,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
        ensure(c, c->atom_struc, sizeof(int) * N) && ensure(c, c->meta, sizeof(StrucMeta) * std::max(nstruc, 1)) &&
        ensure(c, c->imgs, sizeof(ImgEntry) * imgs.size()) && ensure(c, c->sfrac, sizeof(float4) * N) && ensure(c, c->sfloor, sizeof(int4) * N) &&
        ensure(c, c->nb_j, sizeof(int) * NC) && ensure(c, c->nb_r, sizeof(float4) * NC) && ensure(c, c->nb_code, sizeof(int) * NC) &&
+       ensure(c, c->nb_t, NC) &&
        ensure(c, c->nb_cnt, sizeof(int) * N) && ensure(c, c->nb_rev, sizeof(int) * NC) && ensure(c, c->orphans, sizeof(int) * N) &&
        ensure(c, c->G, sizeof(float) * N * c->gstride) && ensure(c, c->dEdG, sizeof(float) * N * c->gstride) &&
        ensure(c, c->eatom, sizeof(float) * N) && ensure(c, c->perm, sizeof(int) * N) &&
@@ -379,6 +380,7 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.nb_j = (int*)c->nb_j.p;
   B.nb_r = (float4*)c->nb_r.p;
   B.nb_code = (int*)c->nb_code.p;
+  B.nb_t = (unsigned char*)c->nb_t.p;
   B.nb_cnt = (int*)c->nb_cnt.p;
   B.nb_rev = (int*)c->nb_rev.p;
   B.ncells = U.ncells;
@@ -581,7 +583,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
-                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom};
+                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);
@@ -740,6 +742,7 @@ int build_skin(nnpgpu_ctx* c, int natoms, const double* posn, const double* cell
   cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * natoms, posn_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
   BatchDev B = batch_view(c, U, (const double*)c->posn.p, nullptr, (double*)c->energy.p, (double*)c->force.p);
   B.rc = rc_skin;
+  B.nb_t = nullptr;  // skin lists keep no species
   B.nb_j = d_j;
   B.nb_code = d_code;
   B.nb_cnt = d_cnt;
