@@ -100,6 +100,8 @@ struct StrucMeta {
   float margin;          // FP32 filter margin on r^2
   int nc[3];             // cell grid (mode 4)
   int pad4;
+  float dmax2f, fro2f;   // FP32 copies of dMax2 and fro^2, and of the shifts, for the FP32 tests
+  float shiftsf[18];
 };
 // One lattice shift of the image box, in the reference's enumeration order (vf = v in FP32).
 struct ImgEntry {
@@ -153,7 +155,12 @@ __device__ __forceinline__ void cell_diff(const StrucMeta& S, double p0, double 
       const double d2 = sqn3(t0, t1, t2);
       if (d2 < dmin2) { dmin2 = d2; r0 = t0; r1 = t1; r2 = t2; best = k; }
     }
-    if (best >= 0) D[best / 2] += (best % 2 == 0) ? -1 : 1;
+    if (best >= 0) {  // constant indices keep D in registers
+      const int step = (best % 2 == 0) ? -1 : 1;
+      if (best < 2) D[0] += step;
+      else if (best < 4) D[1] += step;
+      else D[2] += step;
+    }
     o0 = r0; o1 = r1; o2 = r2;
   }
 }

@@ -3,11 +3,32 @@
 // NNP::force (src/nnp/nnp.cpp:416-482) adds each neighbour-slot contribution W to the centre
 // atom and subtracts it from the neighbour only when the slot is the neighbour's minimum image.
 // Here F_j = sum_{s in list(j)} W[j,s] - sum_{s in list(j), min} W[rev(j,s)], where rev is the
-// transposed slot built by reverse_kernel: a gather over the atom's own list, FP64, no atomics.
+// transposed slot built by reverse_kernel: a gather over the atom's own list, no atomics.
+// Each lane sums its few slots without rounding loss as an unevaluated pair hi + lo of floats
+// (TwoSum, Knuth; the pair carries about 48 bits), and the lanes' pairs are added in FP64.  The
+// FP64 pipe (1/64 of the FP32 rate on GB300) then sees a few operations per atom instead of
+// two per slot and component.
 #include "common.cuh"
 #include "kernels.h"
 
 namespace nnpgpu {
+
+// s + e == a + b exactly (TwoSum; correctly rounded adds, no contraction)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+struct PairSum {
+  float hi = 0.f, lo = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float s, e;
+    two_sum(hi, x, s, e);
+    hi = s;
+    lo = __fadd_rn(lo, e);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
 
 __global__ void __launch_bounds__(128) gather_kernel(int a0, int natoms, int cap, const int* __restrict__ nb_code,
                                                      const int* __restrict__ nb_cnt, const int* __restrict__ nb_rev,
@@ -16,26 +37,26 @@ __global__ void __launch_bounds__(128) gather_kernel(int a0, int natoms, int cap
   const int j = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (j >= a0 + natoms) return;
   const int n = min(nb_cnt[j], cap);
-  double fx = 0, fy = 0, fz = 0;
+  PairSum sx, sy, sz;
   for (int s = lane; s < n; s += 32) {
     const size_t g = (size_t)j * cap + s;
     const float4 w = W[g];
-    fx += w.x;
-    fy += w.y;
-    fz += w.z;
+    sx.add(w.x);
+    sy.add(w.y);
+    sz.add(w.z);
     if (code_min(nb_code[g])) {
       const int r = nb_rev[g];
       if (r >= 0) {
         const float4 v = W[r];
-        fx -= v.x;
-        fy -= v.y;
-        fz -= v.z;
+        sx.add(-v.x);
+        sy.add(-v.y);
+        sz.add(-v.z);
       }
     }
   }
-  fx = warp_sum_d(fx);
-  fy = warp_sum_d(fy);
-  fz = warp_sum_d(fz);
+  const double fx = warp_sum_d(sx.value());
+  const double fy = warp_sum_d(sy.value());
+  const double fz = warp_sum_d(sz.value());
   if (lane == 0) {
     force[3 * (size_t)j] = fx;
     force[3 * (size_t)j + 1] = fy;

@@ -160,19 +160,24 @@ __device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& 
   rf_mul(S, d[0], d[1], d[2], o0, o1, o2);
   const float m = S.margin;
   const float n2 = o0 * o0 + o1 * o1 + o2 * o2;
-  const float dmax2 = (float)S.dMax2;
+  const float dmax2 = S.dmax2f;
   if (fabsf(n2 - dmax2) <= m) ok = false;
   if (n2 > dmax2) {
     float best = n2, second = 3.4e38f, b0 = o0, b1 = o1, b2 = o2;
     int bk = -1;
     for (int k = 0; k < 6; ++k) {
-      const float t0 = o0 + (float)S.shifts[3 * k], t1 = o1 + (float)S.shifts[3 * k + 1], t2 = o2 + (float)S.shifts[3 * k + 2];
+      const float t0 = o0 + S.shiftsf[3 * k], t1 = o1 + S.shiftsf[3 * k + 1], t2 = o2 + S.shiftsf[3 * k + 2];
       const float q = t0 * t0 + t1 * t1 + t2 * t2;
       if (q < best) { second = best; best = q; b0 = t0; b1 = t1; b2 = t2; bk = k; }
       else if (q < second) second = q;
     }
     if (second - best <= m) ok = false;
-    if (bk >= 0) D[bk / 2] += (bk % 2 == 0) ? -1 : 1;
+    if (bk >= 0) {  // constant indices keep D in registers
+      const int step = (bk % 2 == 0) ? -1 : 1;
+      if (bk < 2) D[0] += step;
+      else if (bk < 4) D[1] += step;
+      else D[2] += step;
+    }
     o0 = b0; o1 = b1; o2 = b2;
   }
   return ok;
@@ -181,11 +186,11 @@ __device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& 
 // Single-image decision (modes 2 and 4) for centre i and candidate j: the Cell::diff image of
 // j is kept when |diff|^2 <= rc^2.  FP32 from the wrapped fractional coordinates, with the FP64
 // replay of Cell::diff when |diff|^2 lies within the margin of rc^2.
-__device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& si, const int4& fi, int j, const float4* __restrict__ sfrac,
+// sj = sfrac[j], loaded by the caller ahead of use.
+__device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& si, const int4& fi, int j, const float4 sj,
                                              const int4* __restrict__ sfloor, const double* __restrict__ posn, double pi0, double pi1,
                                              double pi2, double rc2, float rc2f, float m, float& r0, float& r1, float& r2, float& dr,
                                              int D[3]) {
-  const float4 sj = sfrac[j];
   const float dl0 = si.x - sj.x, dl1 = si.y - sj.y, dl2 = si.z - sj.z;
   int k0, k1, k2;
   const float q0 = round_even(dl0, k0), q1 = round_even(dl1, k1), q2 = round_even(dl2, k2);
@@ -244,13 +249,16 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
     // single image: keep the Cell::diff image if |diff|^2 <= rc^2 (the only shift is zero)
     const float4 si = sfrac[i];
     const int4 fi = sfloor[i];
+    float4 sn = lane < nj ? sfrac[j0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);  // one chunk ahead
     for (int c = 0; c < nj; c += 32) {
       const int jl = c + lane;
       const int j = j0 + jl;
+      const float4 sj = sn;
+      if (jl + 32 < nj) sn = sfrac[j + 32];
       bool keep = false;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       int D[3] = {0, 0, 0};
-      if (jl < nj && j != i) keep = single_image(S, si, fi, j, sfrac, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
+      if (jl < nj && j != i) keep = single_image(S, si, fi, j, sj, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc, ot, sfrac);
       count += __popc(mk);
@@ -322,26 +330,35 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
     __syncwarp();
     const float4 si = sfrac[i];
     const int4 fi = sfloor[i];
+    // candidate qd -> atom: last range with prefix <= qd, then its slice of cell_atoms
+    auto candidate = [&](int qd) -> int {
+      int lo = 0, hi = nr - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (rp[mid] <= qd) lo = mid;
+        else hi = mid - 1;
+      }
+      return cell_atoms[rb[lo] + qd - rp[lo]];
+    };
+    // the next chunk's candidates and coordinates are fetched while this chunk is decided
+    int jn = lane < total ? candidate(lane) : -1;
+    float4 sn = jn >= 0 ? sfrac[jn] : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c = 0; c < total; c += 32) {
-      const int qd = c + lane;
+      const int j = jn;
+      const float4 sj = sn;
+      const int qn = c + 32 + lane;
+      if (qn < total) {
+        jn = candidate(qn);
+        sn = sfrac[jn];
+      }
       bool keep = false;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       int D[3] = {0, 0, 0};
-      int j = -1;
-      if (qd < total) {
-        int lo = 0, hi = nr - 1;  // last range with prefix <= qd
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (rp[mid] <= qd) lo = mid;
-          else hi = mid - 1;
-        }
-        j = cell_atoms[rb[lo] + qd - rp[lo]];
-        if (j != i) keep = single_image(S, si, fi, j, sfrac, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
-      }
+      if (c + lane < total && j != i) keep = single_image(S, si, fi, j, sj, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       const int slot = count + __popc(mk & lt);
       if (keep && slot < cap) {
-        st_j[slot] = j | (__float_as_int(sfrac[j].w) << 30);  // species in the top two bits
+        st_j[slot] = j | (__float_as_int(sj.w) << 30);  // species in the top two bits
         st_r[slot] = make_float4(r0, r1, r2, dr);
         st_c[slot] = pack_code(D[0], D[1], D[2], true);
       }
@@ -478,7 +495,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
           }
           if (ok && second - mn <= m) ok = false;
           // the reference seeds the minimum search with |R|_F (neighbor.cpp:132)
-          if (ok && best >= 0 && mn >= (float)(S.fro * S.fro) - m) ok = false;
+          if (ok && best >= 0 && mn >= S.fro2f - m) ok = false;
         }
         if (!ok) {
           exact = true;

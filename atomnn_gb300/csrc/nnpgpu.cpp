@@ -144,6 +144,9 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
       m.shifts[6 * c + 3 + r] = -col[c][r];
     }
   for (int k = 0; k < 9; ++k) m.Rf[k] = (float)m.R[k];
+  for (int k = 0; k < 18; ++k) m.shiftsf[k] = (float)m.shifts[k];
+  m.dmax2f = (float)m.dMax2;
+  m.fro2f = (float)(fro * fro);
   // image shells (NeighborList::build, src/struc/neighbor.cpp:70-95), lattice vectors sorted
   // by decreasing norm with a stable order for ties
   int perm[3] = {0, 1, 2};

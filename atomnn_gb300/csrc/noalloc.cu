@@ -121,6 +121,9 @@ int fixed_meta(const double* cell, int natoms, double rc, StrucMeta& m, ImgEntry
       m.shifts[6 * q + 3 + r] = -col[q][r];
     }
   for (int k = 0; k < 9; ++k) m.Rf[k] = (float)m.R[k];
+  for (int k = 0; k < 18; ++k) m.shiftsf[k] = (float)m.shifts[k];
+  m.dmax2f = (float)m.dMax2;
+  m.fro2f = (float)(fro * fro);
   int perm[3] = {0, 1, 2};  // columns by decreasing norm, stable for ties
   for (int a = 1; a < 3; ++a)
     for (int b = a; b > 0 && nrm3(col[perm[b]]) > nrm3(col[perm[b - 1]]); --b) {

@@ -209,6 +209,7 @@ def main():
     ap.add_argument("--ref-step-atoms", type=int, default=0)
     ap.add_argument("--count", type=int, default=512, help="structures of the workload (512 = the full workload)")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     args = ap.parse_args()
@@ -296,7 +297,10 @@ def main():
     head_flags = batched | (E.BF16 if bf16_ok else 0)
     # launch shapes (atoms per CTA of the neighbour / descriptor / chain-rule kernels) picked by
     # the engine's autotuner on this workload before anything is timed
-    tune_shapes, tune_report = eng.autotune(natoms, posn, species, cells, (E.BF16 if bf16_ok else 0) | E.FORCE)
+    if args.no_autotune:
+        tune_shapes, tune_report = eng.get_tune(), "not run (--no-autotune)"
+    else:
+        tune_shapes, tune_report = eng.autotune(natoms, posn, species, cells, (E.BF16 if bf16_ok else 0) | E.FORCE)
 
     clocks = ClockSampler(local)
     ms, prof = timed(head_flags, args.steps, args.warmup, profile=True)

@@ -296,3 +296,39 @@ def test_autotune_keeps_results(native_lib):
                 np.testing.assert_array_equal(a, b)
     finally:
         eng.close()
+
+
+@pytest.mark.parametrize("variant", ["all_moment_blocks", "lambda_above_one"])
+def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant):
+    """Blocks with zeta <= 4 and |lambda| <= 1 run through the moment tensors, the others
+    through the triplet loop.  all_moment_blocks: every block (the same-species A-A block
+    included) on the moment path; lambda_above_one: lambda = 1.5 forces the triplet loop on
+    low-zeta blocks.  Both against the oracle on structures with one, few and many neighbours."""
+    from atomnn_gb300 import engine
+    pot = W.make_potential("mixed512")
+    for (i, j, k), b in list(pot.angular.items()):
+        if variant == "all_moment_blocks":
+            pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [1, -1])
+        elif j != k:
+            pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [1.5, -1])
+    for t in range(2):  # input sizes changed: new networks
+        means = W._estimate_means(pot, t, 0.07, [1.0 / 3.0, 2.0 / 3.0])
+        pot.nets[t] = W._make_network(np.random.default_rng(t), pot.ninput(t), [64, 64], means)
+    path = str(tmp_path / "variant.nnp")
+    W.write_potential(pot, path)
+    eng = engine.Engine(path)
+    orc = oracle_lib.OracleNNP(path)
+    try:
+        strucs = W.make_structures("mixed512", seed=17, count=4, sizes=[20, 90, 400, 1200])
+        strucs.append(W.Structure(posn=np.array([[0.0, 0.0, 0.0], [1.9, 0.4, 0.2], [0.3, 2.1, 0.1]]),
+                                  species=np.array([0, 1, 0], np.int32), cell=np.zeros((3, 3))))
+        e, F, G = eng.compute(strucs, _flags("ENERGY", "FORCE", "SYMM", "BATCHED"))
+        off = 0
+        for k, s in enumerate(strucs):
+            eo, Fo, Go = orc.compute(s.posn, s.species, s.cell, force=True, symm=True)
+            _assert_ef(e[k], F[k], eo, Fo, s.natoms)
+            Gs = G[off:off + s.natoms, :Go.shape[1]]
+            off += s.natoms
+            np.testing.assert_allclose(Gs, Go, rtol=0, atol=G_TOL * max(np.abs(Go).max(), 1e-30))
+    finally:
+        eng.close()
