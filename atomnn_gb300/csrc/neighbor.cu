@@ -493,7 +493,9 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
               }
             }
           }
-          if (ok && second - mn <= m) ok = false;
+          // a near tie between the two closest kept images could flip the minimum-image flag;
+          // with fewer than two kept images (or for the self pair) there is no tie to resolve
+          if (ok && best >= 0 && second < 3.0e38f && second - mn <= m) ok = false;
           // the reference seeds the minimum search with |R|_F (neighbor.cpp:132)
           if (ok && best >= 0 && mn >= S.fro2f - m) ok = false;
         }
