@@ -10,9 +10,16 @@
 
 namespace nnpgpu {
 
+// One atomic per warp and species (ballot + popc) instead of one per atom: a batch has a
+// handful of species, so per-atom atomics would all hit the same few counters.
 __global__ void type_count_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, int* __restrict__ tc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < natoms) atomicAdd(&tc[clamp_type(type[a0 + i], ntypes)], 1);
+  const int lane = threadIdx.x & 31;
+  const int t = i < natoms ? clamp_type(type[a0 + i], ntypes) : -1;
+  for (int tt = 0; tt < ntypes; ++tt) {
+    const unsigned m = __ballot_sync(0xffffffffu, t == tt);
+    if (lane == 0 && m) atomicAdd(&tc[tt], __popc(m));
+  }
 }
 // tc[0..NT) counts -> exclusive offsets in tc[NT_MAX+1 .. 2*NT_MAX+1], cursors in tc[2*NT_MAX+2 ..]
 __global__ void type_offsets_kernel(int ntypes, int* __restrict__ tc) {
@@ -28,7 +35,15 @@ __global__ void type_offsets_kernel(int ntypes, int* __restrict__ tc) {
 }
 __global__ void type_scatter_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, int* __restrict__ tc, int* __restrict__ perm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < natoms) perm[atomicAdd(&tc[2 * NT_MAX + 2 + clamp_type(type[a0 + i], ntypes)], 1)] = a0 + i;
+  const int lane = threadIdx.x & 31;
+  const int t = i < natoms ? clamp_type(type[a0 + i], ntypes) : -1;
+  for (int tt = 0; tt < ntypes; ++tt) {
+    const unsigned m = __ballot_sync(0xffffffffu, t == tt);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&tc[2 * NT_MAX + 2 + tt], __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (t == tt) perm[base + __popc(m & ((1u << lane) - 1u))] = a0 + i;
+  }
 }
 
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st) {
