@@ -22,11 +22,15 @@ constexpr int NLAYER_MAX = 4;                      // network layers (hidden + o
 constexpr int HID_MAX = 256;                       // nodes per layer
 
 enum { CUT_STEP = 1, CUT_COS = 2, CUT_TANH = 3 };
+// radial families (PhiRN, src/nnp/basis_radial.hpp:25-33) and angular pair factors (PhiAN,
+// src/nnp/basis_angular.hpp:25-32)
+enum { RAD_GAUSSIAN = 1, RAD_TANH = 2, RAD_SOFTPLUS = 3, RAD_LOGCOSH = 4, RAD_SWISH = 5, RAD_MISH = 6 };
+enum { ANG_GAUSS = 1, ANG_IPOWP = 2, ANG_IPOWS = 3, ANG_SECHP = 4, ANG_SECHS = 5 };
 enum { ACT_LINEAR = 1, ACT_SIGMOID = 2, ACT_TANH = 3 };
 
 // Radial basis of centre type I against neighbour type J (BasisR, src/nnp/basis_radial.hpp:53-94).
 struct RadialP {
-  int n, off, cut, pad;
+  int n, off, cut, phi;
   float rc, pirc, rci, norm;
   float rs[NR_MAX], eta[NR_MAX];
 };

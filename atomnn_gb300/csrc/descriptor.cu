@@ -85,8 +85,8 @@ __device__ const signed char c_mom_up[MOM_Q][3] = {{1, 2, 3},    {4, 5, 6},    {
                                                    {11, 13, 14}, {12, 14, 15}, {13, 16, 17}, {14, 17, 18}, {15, 18, 19},
                                                    {20, 21, 22}, {21, 23, 24}, {22, 24, 25}, {23, 26, 27}, {24, 27, 28},
                                                    {25, 28, 29}, {26, 30, 31}, {27, 31, 32}, {28, 32, 33}, {29, 33, 34}};
-// binomial(zeta, n) for zeta = 1, 2, 4
-__device__ const float c_mom_binom[3][MOM_N + 1] = {{1, 1, 0, 0, 0}, {1, 2, 1, 0, 0}, {1, 4, 6, 4, 1}};
+// binomial(zeta, n) / 2^zeta for zeta = 1, 2, 4
+__device__ const float c_mom_binom[3][MOM_N + 1] = {{0.5f, 0.5f, 0, 0, 0}, {0.25f, 0.5f, 0.25f, 0, 0}, {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f}};
 
 // Moments of nsets slot ranges (set 0: [lo0,hi0), set 1: [lo1,hi1)) for every width of the block:
 // M[(set*ne + e)*MOM_C + r] = sum over the set's slots of w_e u^(a,b,c).  Each (set, width) pair
@@ -163,11 +163,11 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nse
   }
 }
 
-// coefficient of cos^n in ((1 + lam cos)/2)^zeta, zeta = 2^m <= 4
+// coefficient of cos^n in ((1 + lam cos)/2)^zeta, zeta = 2^m <= 4: binomial / 2^zeta * lam^n
 __device__ __forceinline__ float mom_coef(int m, float lam, int n) {
   float lp = 1.f;
   for (int k = 0; k < n; ++k) lp *= lam;
-  return c_mom_binom[m][n] * lp * (1.0f / (float)(1 << (1 << m)));
+  return c_mom_binom[m][n] * lp;
 }
 
 // G4 of a moment block (BasisA::symm summed as in NNP::symm, nnp.cpp:359-377)
@@ -204,7 +204,7 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool s
       v = fmaf(c_mom_binom[m][n] * lp, V[e * (MOM_N + 1) + n], v);
       lp *= lam;
     }
-    Gi[A.off + f] = A.norm * v * (1.0f / (float)(1 << zeta));
+    Gi[A.off + f] = A.norm * v;
   }
   __syncwarp();
 }
@@ -246,7 +246,7 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
 #pragma unroll
           for (int bb = n - a; bb >= 0; --bb) {
             const int c = n - a - bb;
-            mono[mom_idx(a, bb, c)] = mom_mult(a, bb, c) * px[a] * (py[bb] * pz[c]);
+            mono[mom_idx(a, bb, c)] = c_mom_mult[mom_idx(a, bb, c)] * px[a] * (py[bb] * pz[c]);
           }
     }
     float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -649,6 +649,62 @@ __device__ void run_block(const WarpSmem& S, const AngP& A, const Sched& sc, int
 #undef NNP_CASE
 }
 
+// Radial function of family phi without the cutoff (BasisR::symm, basis_radial.cpp:302-364), with
+// x = r - rs and arg = -eta x; FP32, exponentials through __expf.
+__device__ __forceinline__ float radial_value(int phi, float eta, float rs, float d) {
+  const float x = d - rs, arg = -eta * x;
+  switch (phi) {
+    case RAD_GAUSSIAN: return __expf(-eta * x * x);
+    case RAD_TANH: return 0.5f * (tanhf(arg) + 1.0f);
+    case RAD_SOFTPLUS: return arg > 0.f ? arg + log1pf(__expf(-arg)) : log1pf(__expf(arg));
+    case RAD_LOGCOSH: return arg > 0.f ? arg + 0.5f * log1pf(__expf(-2.0f * arg)) : 0.5f * log1pf(__expf(2.0f * arg));
+    case RAD_SWISH:
+      if (arg > 0.f) { const float e = __expf(-arg); return arg / (1.0f + e); }
+      if (arg < 0.f) { const float e = __expf(arg); return arg * e / (1.0f + e); }
+      return 0.f;
+    default:  // RAD_MISH
+      if (arg > 0.f) { const float e = __expf(-arg); return arg * (2.0f * e + 1.0f) / (2.0f * e * (e + 1.0f) + 1.0f); }
+      if (arg < 0.f) { const float e = __expf(arg); return arg * e * (e + 2.0f) / (e * (e + 2.0f) + 2.0f); }
+      return 0.f;
+  }
+}
+
+// The per-function term of BasisR::force (basis_radial.cpp:371-444): amp -= dE/dG_i times this,
+// the reference's expressions for each family (cut, gcut: cutoff value and derivative).
+__device__ __forceinline__ float radial_force_term(int phi, float eta, float rs, float d, float cut, float gcut) {
+  const float x = d - rs, arg = -eta * x;
+  switch (phi) {
+    case RAD_GAUSSIAN: return __expf(-eta * x * x) * (-2.0f * eta * x * cut + gcut);
+    case RAD_TANH: {
+      const float t = tanhf(arg);
+      return 0.5f * (-eta * (1.0f - t * t) * cut + (1.0f + t) * gcut);
+    }
+    case RAD_SOFTPLUS:
+      if (arg > 0.f) { const float e = __expf(-arg); return -eta / (1.0f + e) * cut + (arg + log1pf(e)) * gcut; }
+      else { const float e = __expf(arg); return -eta * e / (1.0f + e) * cut + log1pf(e) * gcut; }
+    case RAD_LOGCOSH:
+      if (arg > 0.f) { const float e = __expf(-2.0f * arg); return -eta / (1.0f + e) * cut + (arg + 0.5f * log1pf(e)) * gcut; }
+      else { const float e = __expf(2.0f * arg); return -eta * e / (1.0f + e) * cut + 0.5f * log1pf(e) * gcut; }
+    case RAD_SWISH:
+      if (arg > 0.f) {
+        const float e = __expf(-arg), den = 1.0f / (1.0f + e);
+        return (-eta * (1.0f + e * (1.0f + arg)) * den * cut + arg * gcut) * den;
+      } else {
+        const float e = __expf(arg), den = 1.0f / (1.0f + e);
+        return (-eta * (1.0f + arg + e) * den * cut + arg * gcut) * e * den;
+      }
+    default:  // RAD_MISH
+      if (arg > 0.f) {
+        const float e = __expf(-arg), den = 1.0f / (2.0f * e * (e + 1.0f) + 1.0f);
+        return (-eta * (1.0f + e * (4.0f + e * (4.0f * arg + 6.0f + e * 4.0f * (arg + 1.0f)))) * den * cut +
+                arg * (2.0f * e + 1.0f) * gcut) * den;
+      } else {
+        const float e = __expf(arg), den = 1.0f / (e * (e + 2.0f) + 2.0f);
+        return (-eta * (e * (e * (e + 4.0f) + 4.0f * arg + 6.0f) + 4.0f * (arg + 1.0f)) * den * cut + arg * (e + 2.0f) * gcut) * den * e;
+      }
+  }
+}
+
 // When every basis of centre type I shares one cutoff function and radius, evaluate it once per
 // staged neighbour (value and derivative into S.fc / S.gc) for all blocks to read.
 __device__ __forceinline__ bool cutoff_cache(const WarpSmem& S, const PotParams& P, int I, int n) {
@@ -701,10 +757,15 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
         float fc, gc;
         if (cc) fc = S.fc[p];
         else cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
+        if (R.phi == RAD_GAUSSIAN) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const float x = d - rs[k];
-          acc[k] = fmaf(__expf(-eta[k] * x * x), fc, acc[k]);
+          for (int k = 0; k < 4; ++k) {
+            const float x = d - rs[k];
+            acc[k] = fmaf(__expf(-eta[k] * x * x), fc, acc[k]);
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[k] = fmaf(radial_value(R.phi, eta[k], rs[k], d), fc, acc[k]);
         }
       }
 #pragma unroll
@@ -768,10 +829,7 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
       }
       float amp = 0.f;
 #pragma unroll 1
-      for (int f = 0; f < R.n; ++f) {
-        const float x = d - R.rs[f], eta = R.eta[f];
-        amp -= sJ[f] * __expf(-eta * x * x) * (-2.0f * eta * x * fc + gc);
-      }
+      for (int f = 0; f < R.n; ++f) amp -= sJ[f] * radial_force_term(R.phi, R.eta[f], R.rs[f], d, fc, gc);
       amp *= R.norm;
       S.wx[p] = amp * S.ux[p];
       S.wy[p] = amp * S.uy[p];

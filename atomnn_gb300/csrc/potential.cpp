@@ -109,7 +109,8 @@ HPot read_potential(const char* path) {
         b.cut = cut_of(tok(h, 2, L));
         b.rc = std::atof(tok(h, 3, L).c_str());
         const std::string phi = tok(h, 4, L);
-        b.phi = phi == "GAUSSIAN" ? 1 : (phi == "TANH" || phi == "SOFTPLUS" || phi == "LOGCOSH" || phi == "SWISH" || phi == "MISH") ? 2 : 0;
+        b.phi = phi == "GAUSSIAN" ? RAD_GAUSSIAN : phi == "TANH" ? RAD_TANH : phi == "SOFTPLUS" ? RAD_SOFTPLUS
+              : phi == "LOGCOSH" ? RAD_LOGCOSH : phi == "SWISH" ? RAD_SWISH : phi == "MISH" ? RAD_MISH : 0;
         if (b.phi == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid radial function type " + phi);
         const int n = std::atoi(tok(h, 5, L).c_str());
         if (b.norm == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid normalization scheme");
@@ -130,7 +131,8 @@ HPot read_potential(const char* path) {
           b.cut = cut_of(tok(h, 2, L));
           b.rc = std::atof(tok(h, 3, L).c_str());
           const std::string phi = tok(h, 4, L);
-          b.phi = phi == "GAUSS" ? 1 : (phi == "IPOWP" || phi == "IPOWS" || phi == "SECHP" || phi == "SECHS") ? 2 : 0;
+          b.phi = phi == "GAUSS" ? ANG_GAUSS : phi == "IPOWP" ? ANG_IPOWP : phi == "IPOWS" ? ANG_IPOWS : phi == "SECHP" ? ANG_SECHP
+                : phi == "SECHS" ? ANG_SECHS : 0;
           if (b.phi == 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid angular function type " + phi);
           const int n = std::atoi(tok(h, 5, L).c_str());
           b.alpha = std::atoi(tok(h, 6, L).c_str());
@@ -221,12 +223,13 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
     for (int J = 0; J < pot.ntypes; ++J) {
       const HBasisR& b = pot.rad[I][J];
       RadialP& r = P.rad[I][J];
-      if (b.phi != 1 && !b.rs.empty()) unsup("radial functions other than GAUSSIAN");
+
       if ((int)b.rs.size() > NR_MAX) unsup("more than " + std::to_string(NR_MAX) + " radial functions per pair");
       if (b.cut == 0) unsup("unknown cutoff function");
       r.n = (int)b.rs.size();
       r.off = pot.offR[I][J];
       r.cut = b.cut;
+      r.phi = b.phi;
       r.rc = (float)b.rc;
       r.pirc = (float)(kPi / b.rc);
       r.rci = (float)(1.0 / b.rc);

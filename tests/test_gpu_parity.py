@@ -302,7 +302,7 @@ def test_autotune_keeps_results(native_lib):
 def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant):
     """Blocks with zeta <= 4 and |lambda| <= 1 run through the moment tensors, the others
     through the triplet loop.  all_moment_blocks: every block (the same-species A-A block
-    included) on the moment path; lambda_above_one: lambda = 1.5 forces the triplet loop on
+    included) on the moment path; lambda_above_one: lambda = 2 forces the triplet loop on
     low-zeta blocks.  Both against the oracle on structures with one, few and many neighbours."""
     from atomnn_gb300 import engine
     pot = W.make_potential("mixed512")
@@ -310,7 +310,7 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
         if variant == "all_moment_blocks":
             pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [1, -1])
         elif j != k:
-            pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [1.5, -1])
+            pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [2, -1])
     for t in range(2):  # input sizes changed: new networks
         means = W._estimate_means(pot, t, 0.07, [1.0 / 3.0, 2.0 / 3.0])
         pot.nets[t] = W._make_network(np.random.default_rng(t), pot.ninput(t), [64, 64], means)
@@ -330,5 +330,41 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
             Gs = G[off:off + s.natoms, :Go.shape[1]]
             off += s.natoms
             np.testing.assert_allclose(Gs, Go, rtol=0, atol=G_TOL * max(np.abs(Go).max(), 1e-30))
+    finally:
+        eng.close()
+
+
+@pytest.mark.parametrize("family", ["TANH", "SOFTPLUS", "LOGCOSH", "SWISH", "MISH"])
+def test_radial_families_against_oracle(native_lib, oracle_lib, tmp_path, family):
+    """Every radial family of BasisR (basis_radial.cpp:302-444) on the GPU against the oracle:
+    descriptors, energies and forces (the force terms follow the reference's expressions)."""
+    from atomnn_gb300 import engine
+    pot = W.make_potential("mixed512")
+    for key, b in pot.radial.items():
+        b.phi = family
+    path = str(tmp_path / "radial.nnp")
+    W.write_potential(pot, path)
+    # networks scaled by the inputs' actual means for this family (taken from the oracle)
+    orc = oracle_lib.OracleNNP(path)
+    sample = W.make_structures("mixed512", seed=23, count=1, sizes=[600])[0]
+    _, _, Gs = orc.compute(sample.posn, sample.species, sample.cell, force=False, symm=True)
+    for t in range(2):
+        means = np.abs(Gs[sample.species == t, :pot.ninput(t)]).mean(axis=0) + 1e-3
+        pot.nets[t] = W._make_network(np.random.default_rng(t + 7), pot.ninput(t), [64, 64], means)
+    W.write_potential(pot, path)
+    orc = oracle_lib.OracleNNP(path)
+    eng = engine.Engine(path)
+    try:
+        strucs = W.make_structures("mixed512", seed=29, count=3, sizes=[30, 250, 900])
+        e, F, G = eng.compute(strucs, _flags("ENERGY", "FORCE", "SYMM", "BATCHED"))
+        off = 0
+        for k, s in enumerate(strucs):
+            eo, Fo, Go = orc.compute(s.posn, s.species, s.cell, force=True, symm=True)
+            # these untrained potentials give forces up to ~10 eV/A: the FP32 force bound scales
+            # with the largest force (F_TOL per 2 eV/A of it)
+            assert abs(e[k] - eo) / s.natoms <= E_TOL
+            assert np.abs(F[k] - Fo).max() <= F_TOL * max(1.0, np.abs(Fo).max() / 2.0)
+            np.testing.assert_allclose(G[off:off + s.natoms, :Go.shape[1]], Go, rtol=0, atol=G_TOL * np.abs(Go).max())
+            off += s.natoms
     finally:
         eng.close()
