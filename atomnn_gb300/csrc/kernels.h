@@ -73,9 +73,14 @@ size_t symm_smem_bytes(int cap, int ne, int warps);
 size_t force_smem_bytes(int cap, int ne, int warps);
 // atomic networks: FP32 SIMT path and BF16 tensor-core path
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st);
+size_t type_sort_ints(int natoms);  // ints of the type_count buffer for a batch of natoms
 void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile, cudaStream_t st);
 int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weights, int ntypes, cudaStream_t st, const void* tcnets_host,
                         int want_grad);
+// the energy trainer's batch error and parameter gradient after a batched energy pass
+int train_tiles(int natoms, int ntypes);
+int launch_train(const BatchDev& B, const NetsP& N, int ntypes, const double* eref, int loss, double delta, double* dcdo, double* err,
+                 float* partial, int pstride, double* grad, int max_params, cudaStream_t st);
 // force gather, orphan fix-up, per-structure energy
 void launch_gather(const BatchDev& B, const NetsP& N, bool add_vacuum, bool want_force, cudaStream_t st);
 

@@ -10,48 +10,100 @@
 
 namespace nnpgpu {
 
-// One atomic per warp and species (ballot + popc) instead of one per atom: a batch has a
-// handful of species, so per-atom atomics would all hit the same few counters.
-__global__ void type_count_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, int* __restrict__ tc) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  const int t = i < natoms ? clamp_type(type[a0 + i], ntypes) : -1;
-  for (int tt = 0; tt < ntypes; ++tt) {
-    const unsigned m = __ballot_sync(0xffffffffu, t == tt);
-    if (lane == 0 && m) atomicAdd(&tc[tt], __popc(m));
-  }
-}
-// tc[0..NT) counts -> exclusive offsets in tc[NT_MAX+1 .. 2*NT_MAX+1], cursors in tc[2*NT_MAX+2 ..]
-__global__ void type_offsets_kernel(int ntypes, int* __restrict__ tc) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    int acc = 0;
-    for (int t = 0; t < ntypes; ++t) {
-      tc[NT_MAX + 1 + t] = acc;
-      tc[2 * NT_MAX + 2 + t] = acc;
-      acc += tc[t];
-    }
-    tc[NT_MAX + 1 + ntypes] = acc;
-  }
-}
-__global__ void type_scatter_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, int* __restrict__ tc, int* __restrict__ perm) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int lane = threadIdx.x & 31;
-  const int t = i < natoms ? clamp_type(type[a0 + i], ntypes) : -1;
-  for (int tt = 0; tt < ntypes; ++tt) {
-    const unsigned m = __ballot_sync(0xffffffffu, t == tt);
-    int base = 0;
-    if (lane == 0 && m) base = atomicAdd(&tc[2 * NT_MAX + 2 + tt], __popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (t == tt) perm[base + __popc(m & ((1u << lane) - 1u))] = a0 + i;
+// Species sort without atomics, so the order is the same on every call: atoms of one species
+// stay in index order.  type_count_kernel counts per block of 256 atoms (warp ballots), the
+// type_offsets_kernel scans the block counts, type_scatter_kernel places each atom
+// at its species offset + its block's offset + its rank within the block.  (The scan runs one
+// warp per species.)
+// Layout of tc: [0, NT) counts, [NT_MAX+1, ...) species offsets, [TC_BLK + b*NT_MAX + t) per-block
+// counts (then per-block offsets).
+constexpr int TC_BLK = 3 * NT_MAX + 3;
+
+__device__ __forceinline__ void block_type_ranks(int t, int ntypes, int* wcnt /* [8][NT_MAX] */, unsigned* mask_out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int tt = 0; tt < NT_MAX; ++tt) {
+    const unsigned m = __ballot_sync(0xffffffffu, t == tt && tt < ntypes);
+    if (lane == 0) wcnt[w * NT_MAX + tt] = __popc(m);
+    if (t == tt) *mask_out = m;
   }
 }
 
+__global__ void __launch_bounds__(256) type_count_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, int* __restrict__ tc) {
+  __shared__ int wcnt[8 * NT_MAX];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = i < natoms ? clamp_type(type[a0 + i], ntypes) : -1;
+  unsigned m = 0;
+  block_type_ranks(t, ntypes, wcnt, &m);
+  __syncthreads();
+  if (threadIdx.x < NT_MAX) {
+    int c = 0;
+    for (int w = 0; w < 8; ++w) c += wcnt[w * NT_MAX + threadIdx.x];
+    tc[TC_BLK + blockIdx.x * NT_MAX + threadIdx.x] = c;
+  }
+}
+// one warp per species: warp-wide exclusive scans over the block counts, 32 blocks at a time
+__global__ void type_offsets_kernel(int ntypes, int nblocks, int* __restrict__ tc) {
+  __shared__ int total[NT_MAX];
+  const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
+  const int* cnt = tc + TC_BLK;
+  int* off = tc + TC_BLK + nblocks * NT_MAX;
+  int run = 0;
+  if (t < ntypes) {
+    for (int b0 = 0; b0 < nblocks; b0 += 32) {
+      const int b = b0 + lane;
+      const int v = b < nblocks ? cnt[b * NT_MAX + t] : 0;
+      int incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int x = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += x;
+      }
+      if (b < nblocks) off[b * NT_MAX + t] = run + incl - v;  // offset within the species for now
+      run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+  }
+  if (lane == 0 && t < NT_MAX) total[t] = t < ntypes ? run : 0;
+  __syncthreads();
+  int base = 0;
+  for (int u = 0; u < t && u < NT_MAX; ++u) base += total[u];
+  if (t < ntypes)
+    for (int b = lane; b < nblocks; b += 32) off[b * NT_MAX + t] += base;
+  if (threadIdx.x < NT_MAX) {
+    int acc = 0;
+    for (int u = 0; u < (int)threadIdx.x; ++u) acc += total[u];
+    tc[threadIdx.x] = total[threadIdx.x];
+    if ((int)threadIdx.x < ntypes) tc[NT_MAX + 1 + threadIdx.x] = acc;
+  }
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int u = 0; u < ntypes; ++u) acc += total[u];
+    tc[NT_MAX + 1 + ntypes] = acc;
+  }
+}
+__global__ void __launch_bounds__(256) type_scatter_kernel(int a0, int natoms, int ntypes, int nblocks, const int* __restrict__ type,
+                                                           const int* __restrict__ tc, int* __restrict__ perm) {
+  __shared__ int wcnt[8 * NT_MAX];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int t = i < natoms ? clamp_type(type[a0 + i], ntypes) : -1;
+  unsigned m = 0;
+  block_type_ranks(t, ntypes, wcnt, &m);
+  __syncthreads();
+  if (t >= 0) {
+    int pos = tc[TC_BLK + nblocks * NT_MAX + blockIdx.x * NT_MAX + t];
+    for (int v = 0; v < w; ++v) pos += wcnt[v * NT_MAX + t];
+    perm[pos + __popc(m & ((1u << lane) - 1u))] = a0 + i;
+  }
+}
+
+size_t type_sort_ints(int natoms) { return TC_BLK + 2 * (size_t)((natoms + 255) / 256) * NT_MAX; }
+
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st) {
   if (B.natoms == 0) return;
-  cudaMemsetAsync(B.type_count, 0, sizeof(int) * (3 * NT_MAX + 3), st);
-  type_count_kernel<<<(B.natoms + 255) / 256, 256, 0, st>>>(B.a0, B.natoms, ntypes, B.type, B.type_count);
-  type_offsets_kernel<<<1, 32, 0, st>>>(ntypes, B.type_count);
-  type_scatter_kernel<<<(B.natoms + 255) / 256, 256, 0, st>>>(B.a0, B.natoms, ntypes, B.type, B.type_count, B.perm);
+  const int nblocks = (B.natoms + 255) / 256;
+  type_count_kernel<<<nblocks, 256, 0, st>>>(B.a0, B.natoms, ntypes, B.type, B.type_count);
+  type_offsets_kernel<<<1, 32 * NT_MAX, 0, st>>>(ntypes, nblocks, B.type_count);
+  type_scatter_kernel<<<nblocks, 256, 0, st>>>(B.a0, B.natoms, ntypes, nblocks, B.type, B.type_count, B.perm);
 }
 
 __device__ __forceinline__ void act_fd(int act, float z, float& a, float& d) {
@@ -213,6 +265,210 @@ void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile
   if (tile <= 16) launch_network_fp32_t<16>(B, N, ntypes, st);
   else if (tile <= 32) launch_network_fp32_t<32>(B, N, ntypes, st);
   else launch_network_fp32_t<64>(B, N, ntypes, st);
+}
+
+}  // namespace nnpgpu
+
+// ------------------------------------------------------------------------------- training
+// The energy trainer's per-batch error and parameter gradient (NNPTE::error,
+// src/nnp/nnpte.cpp:870-921, with Cost::grad, src/ml/nn.cpp:1554-1589).  Descriptors and
+// atomic energies come from the regular batched pass; then
+//   train_loss_kernel   per structure dE = (E - E_ref)/N, the loss, dc/dout = dloss/d(dE) / N;
+//   train_grad_kernel   per tile of TILE atoms of one species: forward pass, back-propagation of
+//                       dc/dout, and the tile's parameter gradient (biases, then weights with the
+//                       input index outer) into its own row of `partial`;
+//   train_reduce_kernel the rows of each species summed in tile order in FP64.
+// No atomics: the result does not depend on scheduling.
+namespace nnpgpu {
+
+__global__ void __launch_bounds__(256) train_loss_kernel(int nstruc, int s0, const StrucMeta* __restrict__ meta,
+                                                         const double* __restrict__ energy, const double* __restrict__ eref, int loss,
+                                                         double delta, double* __restrict__ dcdo, double* __restrict__ err) {
+  __shared__ double r0[256], r1[256];
+  double l0 = 0.0, l1 = 0.0;
+  for (int s = threadIdx.x; s < nstruc; s += blockDim.x) {
+    const int n = meta[s0 + s].natoms;
+    const double norm = n > 0 ? 1.0 / n : 0.0;
+    const double dE = (energy[s] - eref[s]) * norm;
+    double g = norm;
+    if (loss == 0) {
+      l0 += 0.5 * dE * dE;
+      g *= dE;
+    } else if (loss == 1) {
+      l0 += fabs(dE);
+      g *= (dE > 0.0) ? 1.0 : ((dE < 0.0) ? -1.0 : 0.0);
+    } else if (loss == 2) {
+      const double arg = dE / delta, sq = sqrt(1.0 + arg * arg);
+      l0 += delta * delta * (sq - 1.0);
+      g *= dE / sq;
+    } else {
+      const double arg = dE / delta, sq = sqrt(1.0 + arg * arg), lg = log(arg + sq);
+      l0 += delta * delta * (1.0 - sq + arg * lg);
+      g *= lg * delta;
+    }
+    l1 += dE * dE;
+    dcdo[s] = g;
+  }
+  r0[threadIdx.x] = l0;
+  r1[threadIdx.x] = l1;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      r0[threadIdx.x] += r0[threadIdx.x + o];
+      r1[threadIdx.x] += r1[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    err[0] = r0[0];
+    err[1] = r1[0];
+  }
+}
+
+// parameters of one network (ANN::size, src/ml/nn.cpp:899-905)
+__host__ __device__ inline int net_params(const NetP& n) {
+  int s = 0;
+  for (int l = 0; l < n.nlayer; ++l) s += n.nodes[l] * (1 + (l == 0 ? n.nin : n.nodes[l - 1]));
+  return s;
+}
+
+template <int TILE>
+__global__ void __launch_bounds__(128) train_grad_kernel(const __grid_constant__ NetsP N, int ntypes, const int* __restrict__ tc,
+                                                         const int* __restrict__ perm, const float* __restrict__ G, int gstride,
+                                                         const int* __restrict__ atom_struc, int s0, const double* __restrict__ dcdo,
+                                                         float* __restrict__ partial, int pstride) {
+  extern __shared__ float sm[];
+  int t = -1, start = 0, cnt = 0, rem = blockIdx.x;
+  for (int ty = 0; ty < ntypes; ++ty) {
+    const int c = tc[ty];
+    const int nt = (c + TILE - 1) / TILE;
+    if (rem < nt) { t = ty; start = tc[NT_MAX + 1 + ty] + rem * TILE; cnt = min(TILE, c - rem * TILE); break; }
+    rem -= nt;
+  }
+  if (t < 0) return;
+  const NetP& net = N.net[t];
+  const int L = net.nlayer, K0 = net.nin;
+  // smem: X0 = scaled inputs [K0][TILE], A[l] activations of hidden layer l, D[l] dc/dz of layer l
+  float* X0 = sm;
+  float* A[NLAYER_MAX];
+  float* D[NLAYER_MAX];
+  float* p = X0 + K0 * TILE;
+  for (int l = 0; l < L - 1; ++l) { A[l] = p; p += net.nodes[l] * TILE; }
+  for (int l = 0; l < L; ++l) { D[l] = p; p += net.nodes[l] * TILE; }
+  for (int w = threadIdx.x; w < K0 * TILE; w += blockDim.x) {
+    const int k = w / TILE, a = w % TILE;
+    X0[w] = a < cnt ? net.inpw[k] * (G[(size_t)perm[start + a] * gstride + k] + net.inpb[k]) : 0.f;
+  }
+  __syncthreads();
+  const float* in = X0;
+  int Kl = K0;
+  for (int l = 0; l < L - 1; ++l) {
+    tile_gemm<TILE>(in, Kl, net.wt[l], net.nodes[l], net.nodes[l], A[l], net.b[l]);
+    __syncthreads();
+    for (int w = threadIdx.x; w < net.nodes[l] * TILE; w += blockDim.x) {
+      float a, d;
+      act_fd(net.act, A[l][w], a, d);
+      A[l][w] = a;
+    }
+    __syncthreads();
+    in = A[l];
+    Kl = net.nodes[l];
+  }
+  // output layer (one linear node): dc/dz = dc/dout * outw
+  for (int a = threadIdx.x; a < TILE; a += blockDim.x)
+    D[L - 1][a] = a < cnt ? (float)dcdo[atom_struc[perm[start + a]] - s0] * net.outw : 0.f;
+  __syncthreads();
+  // dc/dz_{l-1} = (W_l^T dc/dz_l) .* a'_{l-1}
+  for (int l = L - 1; l > 0; --l) {
+    tile_gemm<TILE>(D[l], net.nodes[l], net.w[l], net.nodes[l - 1], net.nodes[l - 1], D[l - 1], nullptr);
+    __syncthreads();
+    for (int w = threadIdx.x; w < net.nodes[l - 1] * TILE; w += blockDim.x) {
+      const float a = A[l - 1][w];
+      const float d = (net.act == ACT_TANH) ? 1.0f - a * a : (net.act == ACT_SIGMOID) ? a * (1.0f - a) : 1.0f;
+      D[l - 1][w] *= d;
+    }
+    __syncthreads();
+  }
+  // the tile's gradient: bias(l, n) = sum_a D[l][n][a]; weight(l, n, m) = sum_a D[l][n][a] X_l[m][a]
+  float* out = partial + (size_t)blockIdx.x * pstride;
+  int nb = 0;
+  for (int l = 0; l < L; ++l) nb += net.nodes[l];
+  const int np = net_params(net);
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    int l = 0, r = q, n, m = -1;
+    if (r < nb) {
+      while (r >= net.nodes[l]) { r -= net.nodes[l]; ++l; }
+      n = r;
+    } else {
+      r -= nb;
+      while (r >= net.nodes[l] * (l == 0 ? K0 : net.nodes[l - 1])) { r -= net.nodes[l] * (l == 0 ? K0 : net.nodes[l - 1]); ++l; }
+      m = r / net.nodes[l];
+      n = r % net.nodes[l];
+    }
+    const float4* d4 = reinterpret_cast<const float4*>(D[l] + n * TILE);
+    float s = 0.f;
+    if (m < 0) {
+#pragma unroll 4
+      for (int v = 0; v < TILE / 4; ++v) {
+        const float4 x = d4[v];
+        s += (x.x + x.y) + (x.z + x.w);
+      }
+    } else {
+      const float4* x4 = reinterpret_cast<const float4*>((l == 0 ? X0 : A[l - 1]) + m * TILE);
+#pragma unroll 4
+      for (int v = 0; v < TILE / 4; ++v) {
+        const float4 x = d4[v], y = x4[v];
+        s = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, s))));
+      }
+    }
+    out[q] = s;
+  }
+}
+
+// grad[goff[t] + q] = sum over the tiles of species t, in tile order, of partial[tile][q]
+__global__ void train_reduce_kernel(const __grid_constant__ NetsP N, int ntypes, int tile, const int* __restrict__ tc,
+                                    const float* __restrict__ partial, int pstride, double* __restrict__ grad) {
+  int t = blockIdx.y, first = 0, goff = 0;
+  if (t >= ntypes) return;
+  for (int ty = 0; ty < t; ++ty) {
+    first += (tc[ty] + tile - 1) / tile;
+    goff += net_params(N.net[ty]);
+  }
+  const int ntiles = (tc[t] + tile - 1) / tile;
+  const int np = net_params(N.net[t]);
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= np) return;
+  double s = 0.0;
+  for (int k = 0; k < ntiles; ++k) s += (double)partial[(size_t)(first + k) * pstride + q];
+  grad[goff + q] = s;
+}
+
+constexpr int TRAIN_TILE = 64;
+
+size_t train_smem_bytes(const NetsP& N, int ntypes) {
+  size_t floats = 0;
+  for (int t = 0; t < ntypes; ++t) {
+    const NetP& n = N.net[t];
+    size_t f = (size_t)n.nin * TRAIN_TILE;
+    for (int l = 0; l < n.nlayer; ++l) f += (size_t)n.nodes[l] * TRAIN_TILE * (l < n.nlayer - 1 ? 2 : 1);
+    floats = floats > f ? floats : f;
+  }
+  return floats * sizeof(float);
+}
+
+int train_tiles(int natoms, int ntypes) { return (natoms + TRAIN_TILE - 1) / TRAIN_TILE + ntypes; }
+
+int launch_train(const BatchDev& B, const NetsP& N, int ntypes, const double* eref, int loss, double delta, double* dcdo, double* err,
+                 float* partial, int pstride, double* grad, int max_params, cudaStream_t st) {
+  train_loss_kernel<<<1, 256, 0, st>>>(B.nstruc, B.s0, B.meta, B.energy, eref, loss, delta, dcdo, err);
+  const size_t smem = train_smem_bytes(N, ntypes);
+  static bool attr = false;
+  if (!attr) attr = cudaFuncSetAttribute(train_grad_kernel<TRAIN_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  if (smem > 200 * 1024) return -1;
+  train_grad_kernel<TRAIN_TILE><<<train_tiles(B.natoms, ntypes), 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride,
+                                                                                    B.atom_struc, B.s0, dcdo, partial, pstride);
+  train_reduce_kernel<<<dim3((max_params + 127) / 128, ntypes), 128, 0, st>>>(N, ntypes, TRAIN_TILE, B.type_count, partial, pstride, grad);
+  return 0;
 }
 
 }  // namespace nnpgpu

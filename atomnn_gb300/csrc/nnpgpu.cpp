@@ -321,7 +321,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
        ensure(c, c->nb_cnt, sizeof(int) * N) && ensure(c, c->nb_rev, sizeof(int) * NC) && ensure(c, c->orphans, sizeof(int) * N) &&
        ensure(c, c->G, sizeof(float) * N * c->gstride) && ensure(c, c->dEdG, sizeof(float) * N * c->gstride) &&
        ensure(c, c->eatom, sizeof(float) * N) && ensure(c, c->perm, sizeof(int) * N) &&
-       ensure(c, c->type_count, sizeof(int) * (3 * NT_MAX + 3)) && ensure(c, c->W, sizeof(float4) * NC) &&
+       ensure(c, c->type_count, sizeof(int) * type_sort_ints((int)N)) && ensure(c, c->W, sizeof(float4) * NC) &&
        ensure(c, c->force, sizeof(double) * 3 * N) && ensure(c, c->energy, sizeof(double) * std::max(nstruc, 1)) &&
        ensure(c, c->status, sizeof(int) * ST_WORDS) && (c->P.mstride == 0 || ensure(c, c->mom, sizeof(float) * N * c->P.mstride));
   if (ok && U.ncells > 0) {
@@ -586,7 +586,8 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
-                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t};
+                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
+                    &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);
@@ -922,6 +923,59 @@ extern "C" int nnpgpu_set_tune(nnpgpu_ctx* c, int warps_nbr, int warps_symm, int
   c->tune.nn_tile = nn_tile;
   drop_graphs(c);  // captured sequences hold the old shapes
   c->shapes_seen.clear();
+  return NNPGPU_OK;
+}
+
+static int net_param_count(const nnpgpu_ctx* c, int t) {
+  const HNet& n = c->pot.nets[t];
+  int s = 0;
+  for (size_t l = 0; l < n.nodes.size(); ++l) s += n.nodes[l] * (1 + (l == 0 ? n.nin : n.nodes[l - 1]));
+  return s;
+}
+
+extern "C" int nnpgpu_nparams(const nnpgpu_ctx* c, int type) {
+  if (!c || type < 0 || type >= c->pot.ntypes) return -1;
+  return net_param_count(c, type);
+}
+
+// The energy trainer's batch error and gradient (NNPTE::error, src/nnp/nnpte.cpp:870-921): one
+// batched energy pass (FP32 networks, energies without the vacuum energies), then the loss and the
+// parameter gradient on the device (network.cu).
+extern "C" int nnpgpu_train_grad(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
+                                 const double* energy_ref, int loss, double delta, double* error, double* grad) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  if (nstruc <= 0 || !energy_ref || !error || !grad) return set_error(c, NNPGPU_ERR_INVALID, "train: invalid arguments");
+  if (loss < 0 || loss > 3) return set_error(c, NNPGPU_ERR_INVALID, "train: loss must be 0 (MSE), 1 (MAE), 2 (HUBER) or 3 (ASINH)");
+  if ((loss >= 2) && !(delta > 0)) return set_error(c, NNPGPU_ERR_INVALID, "train: HUBER and ASINH need delta > 0");
+  for (int s = 0; s < nstruc; ++s)
+    if (!natoms || natoms[s] <= 0) return set_error(c, NNPGPU_ERR_INVALID, "train: every structure needs atoms");
+  std::vector<double> e(nstruc);
+  int rc = compute_impl(c, nstruc, natoms, posn, species, cell, NNPGPU_ENERGY | NNPGPU_BATCHED | NNPGPU_NO_VACUUM, e.data(), nullptr,
+                        nullptr, false, nullptr);
+  if (rc != NNPGPU_OK) return rc;
+  cudaStream_t st = c->stream;
+  int total = 0, maxp = 0;
+  for (int t = 0; t < c->pot.ntypes; ++t) {
+    total += net_param_count(c, t);
+    maxp = std::max(maxp, net_param_count(c, t));
+  }
+  const int pstride = (maxp + 3) / 4 * 4;
+  const Uploaded& U = c->meta_cache.U;
+  const int tiles = train_tiles(U.natoms, c->pot.ntypes);
+  if (!ensure(c, c->tr_eref, sizeof(double) * nstruc) || !ensure(c, c->tr_dcdo, sizeof(double) * nstruc) ||
+      !ensure(c, c->tr_err, sizeof(double) * 2) || !ensure(c, c->tr_part, sizeof(float) * (size_t)tiles * pstride) ||
+      !ensure(c, c->tr_grad, sizeof(double) * total))
+    return set_error(c, NNPGPU_ERR_OOM, "train: device allocation failed or HBM budget exceeded");
+  BatchDev B = batch_view(c, U, (const double*)c->posn.p, (const int*)c->type.p, (double*)c->energy.p, (double*)c->force.p);
+  cudaMemcpyAsync(c->tr_eref.p, energy_ref, sizeof(double) * nstruc, cudaMemcpyHostToDevice, st);
+  if (launch_train(B, c->nets, c->pot.ntypes, (const double*)c->tr_eref.p, loss, delta, (double*)c->tr_dcdo.p, (double*)c->tr_err.p,
+                   (float*)c->tr_part.p, pstride, (double*)c->tr_grad.p, maxp, st) != 0)
+    return set_error(c, NNPGPU_ERR_UNSUPPORTED, "train: networks too wide for the gradient kernel's shared memory");
+  cudaMemcpyAsync(error, c->tr_err.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(grad, c->tr_grad.p, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+  const cudaError_t err = cudaStreamSynchronize(st);
+  if (err != cudaSuccess) return cuda_fail(c, err, "train");
   return NNPGPU_OK;
 }
 

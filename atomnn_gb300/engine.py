@@ -19,7 +19,7 @@ EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntype
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
            "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
-           "nnpgpu_md_state", "nnpgpu_md_destroy"]
+           "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad"]
 
 _lib = None
 
@@ -70,6 +70,8 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_md_forces.argtypes = [vp, vp]
     L.nnpgpu_md_run.argtypes = [vp, ip, vp, vp]
     L.nnpgpu_md_state.argtypes = [vp, vp, vp, vp, vp]
+    L.nnpgpu_nparams.argtypes = [vp, ip]
+    L.nnpgpu_train_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, ip, dp, vp, vp]
     L.nnpgpu_md_destroy.argtypes = [vp]
     L.nnpgpu_md_destroy.restype = None
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
@@ -185,6 +187,25 @@ class Engine:
 
     def set_tune(self, warps_nbr=4, warps_symm=4, warps_force=4, nn_tile=32):
         self._check(self.lib.nnpgpu_set_tune(self._ctx, warps_nbr, warps_symm, warps_force, nn_tile))
+
+    # ---- training: batch error and parameter gradient of the energy loss
+    LOSS = {"MSE": 0, "MAE": 1, "HUBER": 2, "ASINH": 3}
+
+    def nparams(self, t):
+        return self.lib.nnpgpu_nparams(self._ctx, t)
+
+    def train_grad(self, structures, energy_ref, loss="MSE", delta=1.0):
+        """(sum of losses, sum of dE^2, gradient) of one batch (nnpgpu_train_grad)."""
+        natoms = np.array([s.posn.shape[0] for s in structures], dtype=np.int32)
+        posn = np.ascontiguousarray(np.concatenate([np.asarray(s.posn, dtype=np.float64) for s in structures]))
+        species = np.ascontiguousarray(np.concatenate([np.asarray(s.species, dtype=np.int32) for s in structures]))
+        cell = np.ascontiguousarray(np.concatenate([_cell_colmajor(s.cell) for s in structures]))
+        eref = np.ascontiguousarray(energy_ref, dtype=np.float64)
+        err = np.zeros(2)
+        grad = np.zeros(sum(self.nparams(t) for t in range(self.ntypes)))
+        self._check(self.lib.nnpgpu_train_grad(self._ctx, len(structures), _p(natoms), _p(posn), _p(species), _p(cell), _p(eref),
+                                               self.LOSS[loss], float(delta), _p(err), _p(grad)))
+        return err[0], err[1], grad
 
     # ---- molecular dynamics on resident device state
     def md(self, struc, mass, dt, skin=1.0, vel=None, flags=0):

@@ -120,6 +120,20 @@ int nnpgpu_profile_enable(nnpgpu_ctx* ctx, int on);
 int nnpgpu_profile_read(const nnpgpu_ctx* ctx, int stage, double* total_ms, long long* count);
 const char* nnpgpu_profile_stage_name(int stage);
 
+/* ---- training: the energy trainer's batch error and parameter gradient.  Replaces the error and
+ * gradient part of NNPTE::error (src/nnp/nnpte.cpp:870-921) with Cost::grad (src/ml/nn.cpp:1554-1589):
+ * per structure E = sum of the atomic network outputs (no vacuum energies), dE = (E - E_ref)/N and
+ * loss 0 MSE dE^2/2, 1 MAE |dE|, 2 HUBER delta^2 (sqrt(1 + (dE/delta)^2) - 1),
+ * 3 ASINH delta^2 (1 - sqrt(1 + x^2) + x asinh x), x = dE/delta.
+ *   energy_ref[nstruc]; error[0] = sum of the losses, error[1] = sum of dE^2;
+ *   grad = the gradient of sum of losses, per species nnpgpu_nparams(ctx, t) values concatenated in
+ *   species order, each in the reference's parameter order (every layer's biases, then every
+ *   layer's weights with the input index outer and the node index inner).
+ * Descriptors are computed from the positions on each call (FP32, FP32 networks). */
+int nnpgpu_nparams(const nnpgpu_ctx* ctx, int type);
+int nnpgpu_train_grad(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* posn, const int* species,
+                      const double* cell, const double* energy_ref, int loss, double delta, double* error, double* grad);
+
 /* ---- launch-shape autotuner (no counterpart in the reference, which has no launch shapes).
  * Times the batched path on the given batch (host buffers, as nnpgpu_compute) for each candidate
  * of each knob - centre atoms (warps) per CTA of the neighbour, descriptor and chain-rule kernels

@@ -310,6 +310,53 @@ struct ANN {
     }
     return out;
   }
+  // ANN::size (src/ml/nn.cpp:899-905): biases of every layer, then weights
+  int size() const {
+    int s = 0;
+    for (int l = 0; l < nlayer(); ++l) s += nodes[l] * (1 + cols(l));
+    return s;
+  }
+  // Cost::grad (src/ml/nn.cpp:1554-1589) after ANN::fpbp: adds dcdo * d out / d parameter into
+  // grad, parameters ordered as the reference stores them: bias(l, n) for every layer, then
+  // weight(l, n, m) with m (the input) outer and n (the node) inner.
+  void param_grad(const double* inp, double dcdo, double* grad) const {
+    const int L = nlayer();
+    std::vector<double> ins(nin);
+    for (int k = 0; k < nin; ++k) ins[k] = inpw[k] * (inp[k] + inpb[k]);
+    std::vector<std::vector<double>> a(L), dadz(L), dcdz(L);
+    for (int l = 0; l < L; ++l) {
+      const int R = nodes[l], C = cols(l);
+      const std::vector<double>& x = (l == 0) ? ins : a[l - 1];
+      a[l].resize(R); dadz[l].resize(R);
+      const int nl = (l == L - 1) ? N_LINEAR : neuron;
+      for (int r = 0; r < R; ++r) {
+        double z = b[l][r];
+        for (int c = 0; c < C; ++c) z += w[l][(size_t)r * C + c] * x[c];
+        act(nl, z, a[l][r], dadz[l][r]);
+      }
+    }
+    dcdz[L - 1].assign(nodes[L - 1], 0.0);
+    for (int r = 0; r < nodes[L - 1]; ++r) dcdz[L - 1][r] = dcdo * outw[r] * dadz[L - 1][r];
+    for (int l = L - 1; l > 0; --l) {
+      const int R = nodes[l], C = cols(l);
+      dcdz[l - 1].assign(C, 0.0);
+      for (int c = 0; c < C; ++c) {
+        double s = 0;
+        for (int r = 0; r < R; ++r) s += w[l][(size_t)r * C + c] * dcdz[l][r];
+        dcdz[l - 1][c] = s * dadz[l - 1][c];
+      }
+    }
+    int count = 0;
+    for (int l = 0; l < L; ++l)
+      for (int n = 0; n < nodes[l]; ++n) grad[count++] += dcdz[l][n];
+    for (int l = 0; l < L; ++l) {
+      const int R = nodes[l], C = cols(l);
+      for (int m = 0; m < C; ++m) {
+        const double x = (l > 0) ? a[l - 1][m] : ins[m];
+        for (int n = 0; n < R; ++n) grad[count++] += dcdz[l][n] * x;
+      }
+    }
+  }
 };
 
 struct NNH {
@@ -914,4 +961,59 @@ extern "C" int oracle_compute(void* nnpv, int natoms, const double* posn, const 
 extern "C" double oracle_network(void* nnpv, int type, const double* symm, double* dedg) {
   NNP& nnp = *(NNP*)nnpv;
   return nnp.nnh[type].nn.fpbp(symm, dedg);
+}
+
+extern "C" int oracle_nnp_nparams(const void* nnp, int type) { return ((const NNP*)nnp)->nnh[type].nn.size(); }
+
+// The per-batch error and gradient of the energy trainer (NNPTE::error, src/nnp/nnpte.cpp:870-921):
+// per structure E = sum of atomic network outputs (no vacuum energies), dE = (E - E_ref)/N, the loss
+// (0 MSE: dE^2/2, 1 MAE: |dE|, 2 HUBER: delta^2 (sqrt(1 + (dE/delta)^2) - 1), 3 ASINH:
+// delta^2 (1 - sqrt(1 + x^2) + x asinh x) with x = dE/delta) and dc/dout = dloss/d(dE) / N;
+// grad (concatenated per type, oracle_nnp_nparams each) += dc/dout * d out/d parameter summed over
+// the structure's atoms (Cost::grad).  error[0] = sum of losses, error[1] = sum of dE^2.
+// symm: the atoms' symmetry functions, one row of `stride` values per atom.
+extern "C" int oracle_train_grad(void* nnpv, int nstruc, const int* natoms, const double* symm, int stride, const int* type,
+                                 const double* eref, int loss, double delta, double* error, double* grad) {
+  try {
+    NNP& nnp = *(NNP*)nnpv;
+    std::vector<size_t> goff(nnp.ntypes + 1, 0);
+    for (int t = 0; t < nnp.ntypes; ++t) goff[t + 1] = goff[t] + nnp.nnh[t].nn.size();
+    for (size_t k = 0; k < goff[nnp.ntypes]; ++k) grad[k] = 0.0;
+    error[0] = error[1] = 0.0;
+    size_t a0 = 0;
+    for (int s = 0; s < nstruc; ++s) {
+      double energy = 0;
+      for (int n = 0; n < natoms[s]; ++n) {
+        const size_t a = a0 + n;
+        energy += nnp.nnh[type[a]].nn.fpbp(symm + a * stride, nullptr);
+      }
+      const double norm = 1.0 / natoms[s];
+      const double dE = (energy - eref[s]) * norm;
+      double dcdo = norm;
+      switch (loss) {
+        case 0: error[0] += 0.5 * dE * dE; dcdo *= dE; break;
+        case 1: error[0] += std::fabs(dE); dcdo *= (dE > 0) ? 1.0 : ((dE < 0) ? -1.0 : 0.0); break;
+        case 2: {
+          const double arg = dE / delta, sq = std::sqrt(1.0 + arg * arg);
+          error[0] += delta * delta * (sq - 1.0);
+          dcdo *= dE / sq;
+        } break;
+        case 3: {
+          const double arg = dE / delta, sq = std::sqrt(1.0 + arg * arg), lg = std::log(arg + sq);
+          error[0] += delta * delta * (1.0 - sq + arg * lg);
+          dcdo *= lg * delta;
+        } break;
+        default: return -1;
+      }
+      error[1] += dE * dE;
+      for (int n = 0; n < natoms[s]; ++n) {
+        const size_t a = a0 + n;
+        nnp.nnh[type[a]].nn.param_grad(symm + a * stride, dcdo, grad + goff[type[a]]);
+      }
+      a0 += natoms[s];
+    }
+    return 0;
+  } catch (...) {
+    return -2;
+  }
 }

@@ -41,6 +41,8 @@ def lib():
         L.oracle_compute.argtypes = [vp, ip, vp, vp, vp, ip, vp, vp, vp, ip]
         L.oracle_network.argtypes = [vp, ip, vp, vp]
         L.oracle_network.restype = dp
+        L.oracle_nnp_nparams.argtypes = [vp, ip]
+        L.oracle_train_grad.argtypes = [vp, ip, vp, vp, ip, vp, vp, ip, dp, vp, vp]
         _lib = L
     return _lib
 
@@ -89,6 +91,28 @@ class OracleNNP:
         if rc != 0:
             raise RuntimeError("oracle_compute failed (%d)" % rc)
         return float(e[0]), F, G
+
+    def train_grad(self, structures, energy_ref, loss=0, delta=1.0):
+        """The energy trainer's batch error and gradient (NNPTE::error, src/nnp/nnpte.cpp:870-921) on
+        the oracle's own FP64 symmetry functions: (sum of losses, sum of dE^2, gradient)."""
+        rows, types, natoms = [], [], []
+        stride = max(self.ninput)
+        for s in structures:
+            _, _, G = self.compute(s.posn, s.species, s.cell, force=False, symm=True)
+            rows.append(G)
+            types.append(np.asarray(s.species, dtype=np.int32))
+            natoms.append(s.posn.shape[0])
+        symm = np.ascontiguousarray(np.concatenate(rows))
+        types = np.ascontiguousarray(np.concatenate(types))
+        natoms = np.asarray(natoms, dtype=np.int32)
+        eref = np.ascontiguousarray(energy_ref, dtype=np.float64)
+        err = np.zeros(2)
+        grad = np.zeros(sum(lib().oracle_nnp_nparams(self._h, t) for t in range(self.ntypes)))
+        rc = lib().oracle_train_grad(self._h, len(natoms), _ptr(natoms), _ptr(symm), stride, _ptr(types), _ptr(eref), int(loss),
+                                     float(delta), _ptr(err), _ptr(grad))
+        if rc != 0:
+            raise RuntimeError("oracle_train_grad failed (%d)" % rc)
+        return err[0], err[1], grad
 
     def network(self, t, g):
         g = np.ascontiguousarray(g, dtype=np.float64)

@@ -151,3 +151,55 @@ def test_nonperiodic_min_flags(oracle_lib):
     nb = oracle_lib.neighbors(6.0, rng.uniform(0, 6, size=(10, 3)), None)
     assert all(not x["min"].any() for x in nb)
     assert sum(len(x["index"]) for x in nb) > 0
+
+
+def _param_slot(pot, t, q):
+    """(kind, layer, node, input) of parameter q of species t in the reference's order: every
+    layer's biases, then every layer's weights with the input index outer (Cost::grad)."""
+    net = pot.nets[t]
+    dims = [net.nin] + list(net.nodes)
+    nb = sum(net.nodes)
+    if q < nb:
+        for l, n in enumerate(net.nodes):
+            if q < n:
+                return "b", l, q, None
+            q -= n
+    q -= nb
+    for l in range(len(net.nodes)):
+        R, C = dims[l + 1], dims[l]
+        if q < R * C:
+            return "w", l, q % R, q // R
+        q -= R * C
+    raise IndexError
+
+
+@pytest.mark.parametrize("loss,delta", [(0, 1.0), (2, 0.05), (3, 0.05), (1, 1.0)])
+def test_train_gradient_matches_finite_differences(oracle_lib, tmp_path, loss, delta):
+    """The trainer's batch gradient (Cost::grad summed as in nnpte.cpp:870-921) equals central
+    differences of its batch loss in single network parameters, for each loss type."""
+    pot = W.make_potential("cell1728")
+    path = str(tmp_path / "p.nnp")
+    W.write_potential(pot, path)
+    strucs = W.make_structures("mixed512", seed=61, count=3, sizes=[12, 20, 16])
+    orc = oracle_lib.OracleNNP(path)
+    e0 = np.array([orc.compute(s.posn, s.species, s.cell, force=False)[0] for s in strucs])
+    eref = e0 + np.array([0.7, -1.3, 2.1])  # the loss is away from its kinks
+    L0, _, grad = orc.train_grad(strucs, eref, loss, delta)
+    nA = pot.nets[0]
+    rng = np.random.default_rng(3)
+    h = 1e-5
+    for t in (0, 1):
+        off = 0 if t == 0 else sum(n * (1 + c) for n, c in zip(nA.nodes, [nA.nin] + list(nA.nodes[:-1])))
+        for q in rng.choice(200, size=4, replace=False).tolist() + [5000 % 9000]:
+            kind, l, n, m = _param_slot(pot, t, q)
+            vals = []
+            for sgn in (1, -1):
+                p2 = W.make_potential("cell1728")
+                if kind == "b":
+                    p2.nets[t].b[l][n] += sgn * h
+                else:
+                    p2.nets[t].w[l][n, m] += sgn * h
+                W.write_potential(p2, path)
+                vals.append(oracle_lib.OracleNNP(path).train_grad(strucs, eref, loss, delta)[0])
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - grad[off + q]) <= 1e-6 + 1e-4 * abs(fd), (t, q, kind, fd, grad[off + q])
