@@ -27,6 +27,8 @@ enum { CUT_STEP = 1, CUT_COS = 2, CUT_TANH = 3 };
 enum { RAD_GAUSSIAN = 1, RAD_TANH = 2, RAD_SOFTPLUS = 3, RAD_LOGCOSH = 4, RAD_SWISH = 5, RAD_MISH = 6 };
 enum { ANG_GAUSS = 1, ANG_IPOWP = 2, ANG_IPOWS = 3, ANG_SECHP = 4, ANG_SECHS = 5 };
 enum { ACT_LINEAR = 1, ACT_SIGMOID = 2, ACT_TANH = 3 };
+// IPOWS and SECHS take r_ij^alpha + r_ik^alpha as one argument; the other families are products
+__host__ __device__ inline bool ang_sum_family(int phi) { return phi == ANG_IPOWS || phi == ANG_SECHS; }
 
 // Radial basis of centre type I against neighbour type J (BasisR, src/nnp/basis_radial.hpp:53-94).
 struct RadialP {
@@ -36,15 +38,17 @@ struct RadialP {
 };
 
 // Angular basis of centre type I against neighbour pair block (J,K) (BasisA,
-// src/nnp/basis_angular.hpp:53-115), GAUSS form.  The block's functions are mapped onto a
-// grid (distinct 1/eta^alpha) x (distinct lambda) x (zeta = 2^m); gidx[f] is the grid cell
-// (e*NL + l)*NZ_MAX + m of file function f.  mom = 1 marks a block evaluated through moment
-// tensors (every zeta <= 4, |lambda| <= 1); its moments start at float moff of the atom's row.
+// src/nnp/basis_angular.hpp:53-115).  The block's functions are mapped onto a grid (distinct
+// 1/eta^alpha) x (distinct lambda) x (zeta = 2^m); gidx[f] is the grid cell
+// (e*NL + l)*NZ_MAX + m of file function f.  phi is the radial factor (ANG_*): GAUSS, IPOWP and
+// SECHP are products h(r_ij) h(r_ik), IPOWS and SECHS functions of r_ij^alpha + r_ik^alpha.
+// mom = 1 marks a block evaluated through moment tensors (a product family, every zeta <= 4,
+// |lambda| <= 1); its moments start at float moff of the atom's row.
 struct AngP {
   int n, off, cut, alpha;
   float rc, pirc, rci, norm;
   int ne, nl, nz, mom;
-  int moff, pad0, pad1, pad2;
+  int moff, phi, pad1, pad2;
   float ietap[NE_MAX];
   float lam[NL];
   signed char gidx[NA_MAX];
@@ -55,7 +59,9 @@ struct PotParams {
   float rc;
   int nin[NT_MAX];
   int mstride;  // floats of moment storage per atom (0: no moment blocks)
-  int pad[3];
+  int kx;       // 1: a triplet-path block of IPOWP or SECHP needs per-pair derivative weights
+  int gen;      // 1: some angular block has a family other than GAUSS
+  int pad;
   // cutoff shared by every basis of centre type I (ccut 0: the bases differ)
   int ccut[NT_MAX];
   float crc[NT_MAX], cpirc[NT_MAX], crci[NT_MAX];
@@ -209,6 +215,26 @@ __device__ __forceinline__ void cutoff_fg(int cut, float d, float rc, float pirc
     f = (d > rc) ? 0.f : 1.f;
     g = 0.f;
   }
+}
+
+// Radial factor of the angular families (BasisA::symm/force, basis_angular.cpp:406-640) at
+// x = ietap * r^alpha (product families) or ietap * (r_ij^alpha + r_ik^alpha) (sum families):
+// returns h(x) and sets kap so that dh/dx = -kap * h.  GAUSS: exp(-x), kap 1; IPOWP/IPOWS:
+// 1/(1+x), kap = h; SECHP/SECHS: sech(x), kap = sqrt(1 - sech^2) = |tanh x| as the reference
+// writes it, here from e = exp(-|x|) without the cancellation of 1 - sech^2.
+__device__ __forceinline__ float ang_h(int phi, float x, float& kap) {
+  if (phi == ANG_IPOWP || phi == ANG_IPOWS) {
+    const float h = 1.0f / (1.0f + x);
+    kap = h;
+    return h;
+  }
+  if (phi == ANG_SECHP || phi == ANG_SECHS) {
+    const float e = __expf(-fabsf(x)), e2 = e * e, den = 1.0f / (1.0f + e2);
+    kap = (1.0f - e2) * den;
+    return 2.0f * e * den;
+  }
+  kap = 1.0f;
+  return __expf(-x);
 }
 
 // species index clamped into the table (invalid input is flagged by frac_kernel)

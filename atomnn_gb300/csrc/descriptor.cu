@@ -11,10 +11,12 @@
 // Exponentials and the cosine cutoff use the hardware approximations (__expf, __sincosf: a few
 // ulp, below the FP32 rounding of the sums they enter).
 //
-// Angular functions (GAUSS, basis_angular.cpp:406-446,456-640) are evaluated on a grid of
-// (distinct eta) x (lambda) x (zeta = 2^m):  exp(-(r_ij^a + r_ik^a)/eta^a) factorises into
-// per-pair terms, ((1+lambda cos)/2)^(2^m) is a chain of squarings, and the force pass needs
-// only three scalars per triplet (d/dcos, d/dr_ij, d/dr_ik of sum_f dE/dG_f G_f).
+// Angular functions (basis_angular.cpp:406-446,456-640) are evaluated on a grid of
+// (distinct eta) x (lambda) x (zeta = 2^m):  the GAUSS factor exp(-(r_ij^a + r_ik^a)/eta^a)
+// (and the IPOWP and SECHP ones) factorise into per-pair terms, ((1+lambda cos)/2)^(2^m) is a
+// chain of squarings, and the force pass needs only three scalars per triplet (d/dcos, d/dr_ij,
+// d/dr_ik of sum_f dE/dG_f G_f).  The sum families IPOWS and SECHS evaluate their factor per
+// triplet.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -23,20 +25,25 @@ namespace nnpgpu {
 constexpr int QMAX = 8;  // owner chunks of 32 per block -> at most 256 neighbours
 
 struct WarpSmem {
-  float *ux, *uy, *uz, *d, *inv, *fc, *gc, *dpa, *ex, *wx, *wy, *wz, *scratch;
+  float *ux, *uy, *uz, *d, *inv, *fc, *gc, *dpa, *ex, *kx, *wx, *wy, *wz, *scratch;
   int *orig, *toff;
 };
 
 // The per-width region ex is at least MOM_EX floats per width so that a moment block's tensors
-// (two sets of MOM_C per width plus the diagonal terms) fit there.
+// (two sets of MOM_C per width plus the diagonal terms) fit there.  With kx, a second per-width
+// region holds the pair factors' derivative weights (IPOWP and SECHP blocks of the force pass).
 __host__ __device__ inline int ex_stride(int cap) { return cap > MOM_EX ? cap : MOM_EX; }
-__host__ __device__ inline size_t warp_smem_floats(int cap, int ne) { return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + 64 + 8; }
+__host__ __device__ inline size_t warp_smem_floats(int cap, int ne, bool kx) {
+  return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + (kx ? (size_t)ne * cap : 0) + 64 + 8;
+}
 
-__device__ inline WarpSmem carve(float* base, int cap, int ne) {
+__device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
   WarpSmem s;
   s.ux = base; s.uy = base + cap; s.uz = base + 2 * cap; s.d = base + 3 * cap; s.inv = base + 4 * cap;
   s.fc = base + 5 * cap; s.gc = base + 6 * cap; s.dpa = base + 7 * cap; s.ex = base + 8 * cap;
   float* w = s.ex + (size_t)ne * ex_stride(cap);
+  s.kx = kx ? w : nullptr;
+  if (kx) w += (size_t)ne * cap;
   s.wx = w; s.wy = w + cap; s.wz = w + 2 * cap;
   s.orig = reinterpret_cast<int*>(w + 3 * cap);
   s.scratch = w + 4 * cap;
@@ -54,7 +61,8 @@ __device__ __forceinline__ float powi(float x, int a) {
 // Blocks whose functions all have zeta <= 4 (and |lambda| <= 1) skip the triplet loop.  The
 // angular term ((1 + lambda cos)/2)^zeta is a polynomial of degree <= 4 in cos = u_j . u_k, and
 //   sum_{j in J, k in K} w_j w_k (u_j . u_k)^n = <M^J_n, M^K_n>,   M^S_n = sum_{j in S} w_j u_j^(x)n,
-// with w = exp(-r^alpha/eta^alpha) f_c(r) (the GAUSS pair factor, basis_angular.cpp:406-421).
+// with w = h(r^alpha/eta^alpha) f_c(r), h the pair factor of a product family (exp(-x) for
+// GAUSS, 1/(1+x) for IPOWP, sech(x) for SECHP; basis_angular.cpp:406-446).
 // The symmetric tensors M_n (n = 0..4) have 35 components in all, so a block costs
 // O(neighbours x 35) instead of O(neighbours^2); J == K blocks take half the full double sum
 // minus its j == k terms (the reference sums j < k, nnp.cpp:359-377).  The chain rule
@@ -93,6 +101,8 @@ __device__ const float c_mom_binom[3][MOM_N + 1] = {{0.5f, 0.5f, 0, 0, 0}, {0.25
 // is summed by its own group of L lanes (L = 32 / pairs, rounded down to a power of two), so the
 // cross-lane reduction takes log2(L) shuffle levels instead of 5.  With Dg, set 0 also gives
 // Dg[e*(MOM_N+1) + n] = sum w_e^2 |u|^2n (the j == k terms of a J == K block).
+// GAUSS instances evaluate exp(-x) directly; the others go through ang_h.
+template <bool GAUSS>
 __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nsets, int lo0, int hi0, int lo1, int hi1,
                               float* __restrict__ M, float* __restrict__ Dg) {
   const int lane = threadIdx.x & 31;
@@ -115,7 +125,8 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nse
     float f, g;
     if (cc) f = S.fc[p];
     else cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
-    const float w = __expf(-ie * powi(d, A.alpha)) * f;
+    float kap;
+    const float w = (GAUSS ? __expf(-ie * powi(d, A.alpha)) : ang_h(A.phi, ie * powi(d, A.alpha), kap)) * f;
     float wx[MOM_N + 1], py[MOM_N + 1], pz[MOM_N + 1];
     wx[0] = w;
     py[0] = 1.f;
@@ -171,6 +182,7 @@ __device__ __forceinline__ float mom_coef(int m, float lam, int n) {
 }
 
 // G4 of a moment block (BasisA::symm summed as in NNP::symm, nnp.cpp:359-377)
+template <bool GEN>
 __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool same, int j0, int nJ, int k0, int nK, float* __restrict__ gmom,
                                float* __restrict__ Gi) {
   const int lane = threadIdx.x & 31;
@@ -178,7 +190,8 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool s
   float* MJ = S.ex;
   float* MK = same ? S.ex : S.ex + nec;
   float* Dg = S.ex + 2 * nec;
-  build_moments(S, A, cc, same ? 1 : 2, j0, j0 + nJ, k0, k0 + nK, MJ, same ? Dg : nullptr);
+  if (!GEN || A.phi == ANG_GAUSS) build_moments<true>(S, A, cc, same ? 1 : 2, j0, j0 + nJ, k0, k0 + nK, MJ, same ? Dg : nullptr);
+  else if constexpr (GEN) build_moments<false>(S, A, cc, same ? 1 : 2, j0, j0 + nJ, k0, k0 + nK, MJ, same ? Dg : nullptr);
   __syncwarp();
   if (gmom) {
     for (int t = lane; t < nec; t += 32) gmom[t] = MJ[t];
@@ -214,6 +227,7 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool s
 // w' u sum_n b_n S_n + (w/r) sum_n n b_n (V_n - (u . V_n) u), and sum_n b_n S_n = b_0 B_0 + u . sum_n b_n V_n.
 // T3[e*MOM_Q + q] holds b_n times the three components of B_n one degree above component q
 // (n = deg q + 1), T0[e] = b_0 B_0; diag adds the j == k term of a J == K block.
+template <bool GAUSS>
 __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, int hi, const float4* __restrict__ T3,
                              const float* __restrict__ T0, const float* __restrict__ b, bool diag) {
   const int lane = threadIdx.x & 31;
@@ -251,9 +265,10 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
     }
     float gx = 0.f, gy = 0.f, gz = 0.f;
     for (int e = 0; e < A.ne; ++e) {
-      const float x = __expf(-A.ietap[e] * da);
+      float kap = 1.0f;
+      const float x = GAUSS ? __expf(-A.ietap[e] * da) : ang_h(A.phi, A.ietap[e] * da, kap);
       const float w = x * f;
-      const float wd = x * (g - A.ietap[e] * dpa);
+      const float wd = x * (g - A.ietap[e] * kap * dpa);
       const float4* __restrict__ Te = T3 + e * MOM_Q;
       float vx[MOM_N], vy[MOM_N], vz[MOM_N];  // b_n V_n per degree n = 1..MOM_N
 #pragma unroll
@@ -302,6 +317,7 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
 }
 
 // chain rule of a moment block (BasisA::force summed as in NNP::force, nnp.cpp:466-478)
+template <bool GEN>
 __device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool same, int j0, int nJ, int k0, int nK,
                                 const float* __restrict__ gmom, const float* __restrict__ gi) {
   const int lane = threadIdx.x & 31;
@@ -333,8 +349,13 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool 
   if (lane < nsets * A.ne) T0[lane] = b[(lane % A.ne) * (MOM_N + 1)] * gmom[(lane / A.ne) * nec + (lane % A.ne) * MOM_C];
   __syncwarp();
   // J's slots against the K moments (J's own for J == K); K's slots against the J moments
-  mom_contract(S, A, cc, j0, j0 + nJ, TK, T0 + (same ? 0 : A.ne), b, same);
-  if (!same) mom_contract(S, A, cc, k0, k0 + nK, TJ, T0, b, false);
+  if (!GEN || A.phi == ANG_GAUSS) {
+    mom_contract<true>(S, A, cc, j0, j0 + nJ, TK, T0 + (same ? 0 : A.ne), b, same);
+    if (!same) mom_contract<true>(S, A, cc, k0, k0 + nK, TJ, T0, b, false);
+  } else if constexpr (GEN) {
+    mom_contract<false>(S, A, cc, j0, j0 + nJ, TK, T0 + (same ? 0 : A.ne), b, same);
+    if (!same) mom_contract<false>(S, A, cc, k0, k0 + nK, TJ, T0, b, false);
+  }
   __syncwarp();
 }
 
@@ -399,19 +420,33 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
   return n;
 }
 
-// Per-pair factors of angular block A for slots [lo,hi): ex[e] = exp(-ietap_e d^alpha)
-// (times the cutoff when with_fc), cutoff value/gradient and alpha d^(alpha-1) fc.
+// Per-pair factors of angular block A for slots [lo,hi): ex[e] = h(ietap_e d^alpha) (times the
+// cutoff when with_fc) and, where the kernel has the region, kx[e] = its derivative weight
+// (ang_h); sum families instead keep d^alpha in ex[p].  Also the cutoff value/gradient and
+// alpha d^(alpha-1) fc.
+template <bool GEN>
 __device__ void block_pair_factors(const WarpSmem& S, const AngP& A, int lo, int hi, int cap, bool with_fc) {
   const int lane = threadIdx.x & 31;
+  const bool sum = GEN && ang_sum_family(A.phi);
   for (int p = lo + lane; p < hi; p += 32) {
     const float d = S.d[p];
     float f, g;
     cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
     const float da = powi(d, A.alpha);
-    for (int e = 0; e < A.ne; ++e) {
-      const float x = __expf(-A.ietap[e] * da);
-      S.ex[e * cap + p] = with_fc ? x * f : x;
-    }
+    if (sum) S.ex[p] = da;
+    else if (!GEN || A.phi == ANG_GAUSS)
+      for (int e = 0; e < A.ne; ++e) {
+        const float x = __expf(-A.ietap[e] * da);
+        S.ex[e * cap + p] = with_fc ? x * f : x;
+        if (S.kx) S.kx[e * cap + p] = 1.0f;
+      }
+    else
+      for (int e = 0; e < A.ne; ++e) {
+        float kap;
+        const float x = GEN ? ang_h(A.phi, A.ietap[e] * da, kap) : 0.f;
+        S.ex[e * cap + p] = with_fc ? x * f : x;
+        if (S.kx) S.kx[e * cap + p] = kap;
+      }
     S.fc[p] = f;
     S.gc[p] = g;
     S.dpa[p] = (float)A.alpha * powi(d, A.alpha - 1) * f;
@@ -625,11 +660,179 @@ __device__ __forceinline__ void force_block(const WarpSmem& S, const AngP& A, co
   }
 }
 
+// G4 sums of a sum-family block (IPOWS, SECHS: basis_angular.cpp:427-441) on the triplet path:
+// the factor h(ietap (r_ij^alpha + r_ik^alpha)) per triplet from ex[p] = r_p^alpha, times the
+// cutoffs in fc.  One instance per kernel (its NE x NZ bounds); widths beyond the block's are
+// skipped.
+template <int NE, int NZ>
+__device__ void symm_block_sum(const WarpSmem& S, const AngP& A, const Sched& sc) {
+  const int lane = threadIdx.x & 31;
+  float acc[NE][NL][NZ];
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) acc[e][l][m] = 0.f;
+  const float lam0 = A.lam[0], lam1 = A.lam[1];
+  for (int q = 0; q * 32 < sc.nown; ++q) {
+    const int x = q * 32 + lane;
+    const int a = sc.xb + min(x, sc.nown - 1);
+    const float uax = S.ux[a], uay = S.uy[a], uaz = S.uz[a], daa = S.ex[a], fa = S.fc[a];
+    for (int dd = sc.d0; dd <= sc.d1; ++dd) {
+      const int nx = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+      if (x < nx) {
+        int y = x + dd;
+        if (y >= sc.mod) y -= sc.mod;
+        const int b = sc.yb + y;
+        const float cs = uax * S.ux[b] + uay * S.uy[b] + uaz * S.uz[b];
+        float p[NL][NZ];
+        p[0][0] = fabsf(0.5f * (1.0f + lam0 * cs));
+        p[1][0] = fabsf(0.5f * (1.0f + lam1 * cs));
+#pragma unroll
+        for (int l = 0; l < NL; ++l)
+#pragma unroll
+          for (int m = 1; m < NZ; ++m) p[l][m] = p[l][m - 1] * p[l][m - 1];
+        const float fab = fa * S.fc[b], s = daa + S.ex[b];
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          if (e >= A.ne) break;
+          float kap;
+          const float E = fab * ang_h(A.phi, A.ietap[e] * s, kap);
+#pragma unroll
+          for (int l = 0; l < NL; ++l)
+#pragma unroll
+            for (int m = 0; m < NZ; ++m) acc[e][l][m] = fmaf(p[l][m], E, acc[e][l][m]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) {
+        const float v = warp_sum(acc[e][l][m]);
+        if (lane == 0) S.scratch[(e * NL + l) * NZ_MAX + m] = v;
+      }
+}
+
+// Chain rule of a block of the non-GAUSS families on the triplet path (BasisA::force,
+// basis_angular.cpp:508-640).  Per triplet and width, the radial factor R and its derivative
+// weights kap_a, kap_b (dR/dr_a = -ietap alpha r_a^(alpha-1) kap_a R): products from the pair
+// regions ex and kx, sums from h(ietap (r_ij^alpha + r_ik^alpha)).  Then
+//   eta0 = -norm f_b (g_a Q - alpha r_a^(alpha-1) f_a Q2a),  Q = sum R q,  Q2a = sum ietap kap_a R q,
+// and likewise eta1; phi as for GAUSS.  One instance per kernel, widths beyond the block's skipped.
+template <int NE, int NZ>
+__device__ void force_block_gen(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  const int lane = threadIdx.x & 31;
+  float sg[NE][NL][NZ];
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) sg[e][l][m] = S.scratch[(e * NL + l) * NZ_MAX + m];
+  const bool sum = ang_sum_family(A.phi);
+  const float lam0 = A.lam[0], lam1 = A.lam[1];
+  const float hn = -0.5f * A.norm, nn = -A.norm;
+  for (int q = 0; q * 32 < sc.nown; ++q) {
+    const int x = q * 32 + lane;
+    const int a = sc.xb + min(x, sc.nown - 1);
+    const float uax = S.ux[a], uay = S.uy[a], uaz = S.uz[a];
+    const float fa = S.fc[a], ga = S.gc[a], pa = S.dpa[a], ia = S.inv[a];
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    for (int dd = sc.d0; dd <= sc.d1; ++dd) {
+      const int nx = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+      if (x < nx) {
+        int y = x + dd;
+        if (y >= sc.mod) y -= sc.mod;
+        const int b = sc.yb + y;
+        const float ubx = S.ux[b], uby = S.uy[b], ubz = S.uz[b];
+        const float fb = S.fc[b], gb = S.gc[b], pb = S.dpa[b], ib = S.inv[b];
+        const float cs = uax * ubx + uay * uby + uaz * ubz;
+        float p[NL][NZ], qd[NL][NZ];
+        p[0][0] = fabsf(0.5f * (1.0f + lam0 * cs));
+        p[1][0] = fabsf(0.5f * (1.0f + lam1 * cs));
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+          qd[l][0] = 1.0f;
+#pragma unroll
+          for (int m = 1; m < NZ; ++m) {
+            qd[l][m] = 2.0f * qd[l][m - 1] * p[l][m - 1];
+            p[l][m] = p[l][m - 1] * p[l][m - 1];
+          }
+        }
+        float Q = 0.f, Q2a = 0.f, Q2b = 0.f, Pp = 0.f;
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          if (e >= A.ne) break;
+          float R, ka, kb;
+          if (sum) {
+            R = ang_h(A.phi, A.ietap[e] * (S.ex[a] + S.ex[b]), ka);
+            kb = ka;
+          } else {
+            R = S.ex[e * cap + a] * S.ex[e * cap + b];
+            ka = S.kx[e * cap + a];
+            kb = S.kx[e * cap + b];
+          }
+          float q0 = 0.f, q1 = 0.f, r0 = 0.f, r1 = 0.f;
+#pragma unroll
+          for (int m = 0; m < NZ; ++m) {
+            q0 = fmaf(sg[e][0][m], p[0][m], q0);
+            q1 = fmaf(sg[e][1][m], p[1][m], q1);
+            r0 = fmaf(sg[e][0][m], qd[0][m], r0);
+            r1 = fmaf(sg[e][1][m], qd[1][m], r1);
+          }
+          const float qe = R * (q0 + q1), ie = A.ietap[e];
+          Q += qe;
+          Q2a = fmaf(ie * ka, qe, Q2a);
+          Q2b = fmaf(ie * kb, qe, Q2b);
+          Pp = fmaf(R, lam0 * r0 + lam1 * r1, Pp);
+        }
+        const float phi = hn * fa * fb * Pp;
+        const float eta0 = nn * fb * (ga * Q - pa * Q2a);
+        const float eta1 = nn * fa * (gb * Q - pb * Q2b);
+        const float Aa = -phi * cs * ia + eta0, Ba = phi * ia;
+        const float Ab = -phi * cs * ib + eta1, Bb = phi * ib;
+        w0 += Aa * uax + Ba * ubx;
+        w1 += Aa * uay + Ba * uby;
+        w2 += Aa * uaz + Ba * ubz;
+        S.wx[b] += Ab * ubx + Bb * uax;
+        S.wy[b] += Ab * uby + Bb * uay;
+        S.wz[b] += Ab * ubz + Bb * uaz;
+      }
+      __syncwarp();
+    }
+    if (x < sc.nown) {
+      S.wx[sc.xb + x] += w0;
+      S.wy[sc.xb + x] += w1;
+      S.wz[sc.xb + x] += w2;
+    }
+    __syncwarp();
+  }
+}
+
 // Dispatch on the block's grid size: eta count 1..NEK, zeta chain length rounded up to 3, 5 or 6
 // (at most NZK).  Only instances within the kernel's bounds are linked, which keeps the
 // kernel's register allocation to what its potential needs.
-template <bool FORCE, int NEK, int NZK>
+// The non-GAUSS families take the one generic instance at the kernel's bounds (their G4 sums
+// for the product families are the GAUSS ones on other pair factors).  Their code is linked
+// only into the GEN kernel instances, launched for potentials that have such blocks: the
+// GAUSS-only instances keep the code size and register allocation of the GAUSS code alone.
+template <bool FORCE, int NEK, int NZK, bool GEN>
 __device__ void run_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  if constexpr (GEN) {
+    if (FORCE && A.phi != ANG_GAUSS) {
+      force_block_gen<NEK, NZK>(S, A, sc, cap);
+      return;
+    }
+    if (!FORCE && ang_sum_family(A.phi)) {
+      symm_block_sum<NEK, NZK>(S, A, sc);
+      return;
+    }
+  }
   const int z = A.nz <= 3 ? 3 : (A.nz <= 5 ? 5 : 6);
   const int key = A.ne * 8 + z;
 #define NNP_CASE(NE_, NZ_)                                   \
@@ -721,7 +924,7 @@ __device__ __forceinline__ bool cutoff_cache(const WarpSmem& S, const PotParams&
 }
 
 // ------------------------------------------------------------------------------------ symm
-template <int NEK, int NZK>
+template <int NEK, int NZK, bool GEN>
 __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                    const int* __restrict__ type, const int* __restrict__ nb_j,
                                                    const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
@@ -731,7 +934,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
-  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, false), cap, NEK, false);
   const int I = clamp_type(type[i], P.ntypes);
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
   const bool cc = cutoff_cache(S, P, I, n);
@@ -784,13 +987,13 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (A.mom) {
-        symm_mom_block(S, A, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
+        symm_mom_block<GEN>(S, A, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
         continue;
       }
-      block_pair_factors(S, A, j0, j0 + nJ, cap, true);
-      if (K != J) block_pair_factors(S, A, k0, k0 + nK, cap, true);
+      block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, true);
+      if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, true);
       __syncwarp();
-      run_block<false, NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
+      run_block<false, NEK, NZK, GEN>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
       for (int f = lane; f < A.n; f += 32) Gi[A.off + f] = A.norm * S.scratch[A.gidx[f]];
       __syncwarp();
@@ -798,7 +1001,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
 }
 
 // ------------------------------------------------------------------------------------ force
-template <int NEK, int NZK>
+template <int NEK, int NZK, bool GEN>
 __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
                                                     const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
@@ -808,7 +1011,8 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
-  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK), cap, NEK);
+  const bool kx = GEN && P.kx;  // a compile-time false in the GAUSS-only instances
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, kx), cap, NEK, kx);
   const int I = clamp_type(type[i], P.ntypes);
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
   const bool cc = cutoff_cache(S, P, I, n);
@@ -847,18 +1051,18 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
       if (A.mom) {
-        force_mom_block(S, A, cc, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
+        force_mom_block<GEN>(S, A, cc, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
         continue;
       }
-      block_pair_factors(S, A, j0, j0 + nJ, cap, false);
-      if (K != J) block_pair_factors(S, A, k0, k0 + nK, cap, false);
+      block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, false);
+      if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, false);
       // dE/dG on the function grid (duplicates of a grid cell add up)
       if (lane == 0) {
         for (int c = 0; c < NE_MAX * NL * NZ_MAX; ++c) S.scratch[c] = 0.f;
         for (int f = 0; f < A.n; ++f) S.scratch[A.gidx[f]] += gi[A.off + f];
       }
       __syncwarp();
-      run_block<true, NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
+      run_block<true, NEK, NZK, GEN>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
     }
 
@@ -867,38 +1071,38 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   for (int p = lane; p < n; p += 32) Wi[S.orig[p]] = make_float4(S.wx[p], S.wy[p], S.wz[p], 0.f);
 }
 
-size_t symm_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne) * warps; }
-size_t force_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne) * warps; }
+size_t symm_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne, false) * warps; }
+size_t force_smem_bytes(int cap, int ne, int warps, bool kx) { return sizeof(float) * warp_smem_floats(cap, ne, kx) * warps; }
 
-template <int NEK, int NZK>
+template <int NEK, int NZK, bool GEN>
 static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
-  if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  symm_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
+  if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  symm_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
 }
-template <int NEK, int NZK>
+template <int NEK, int NZK, bool GEN>
 static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
-  if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  force_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps), st>>>(
+  if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  force_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps, GEN && P.kx), st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
 }
 
 // Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).
 int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st) {
   if (B.natoms == 0) return 0;
-  if (ne <= 2 && nz <= 5) launch_symm_t<2, 5>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 5) launch_symm_t<4, 5>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 6) launch_symm_t<4, 6>(B, P, warps, st);
+  if (ne <= 2 && nz <= 5) P.gen ? launch_symm_t<2, 5, true>(B, P, warps, st) : launch_symm_t<2, 5, false>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 5) P.gen ? launch_symm_t<4, 5, true>(B, P, warps, st) : launch_symm_t<4, 5, false>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 6) P.gen ? launch_symm_t<4, 6, true>(B, P, warps, st) : launch_symm_t<4, 6, false>(B, P, warps, st);
   else return -1;
   return 0;
 }
 int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st) {
   if (B.natoms == 0) return 0;
-  if (ne <= 2 && nz <= 5) launch_force_t<2, 5>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 5) launch_force_t<4, 5>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 6) launch_force_t<4, 6>(B, P, warps, st);
+  if (ne <= 2 && nz <= 5) P.gen ? launch_force_t<2, 5, true>(B, P, warps, st) : launch_force_t<2, 5, false>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 5) P.gen ? launch_force_t<4, 5, true>(B, P, warps, st) : launch_force_t<4, 5, false>(B, P, warps, st);
+  else if (ne <= 4 && nz <= 6) P.gen ? launch_force_t<4, 6, true>(B, P, warps, st) : launch_force_t<4, 6, false>(B, P, warps, st);
   else return -1;
   return 0;
 }

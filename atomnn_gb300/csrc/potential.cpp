@@ -241,13 +241,15 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
       AngP& a = P.ang[I][q];
       const int n = (int)b.eta.size();
       if (n == 0) continue;
-      if (b.phi != 1) unsup("angular functions other than GAUSS");
+      if (b.phi < ANG_GAUSS || b.phi > ANG_SECHS) unsup("unknown angular function");
       if (n > NA_MAX) unsup("more than " + std::to_string(NA_MAX) + " angular functions per block");
       if (b.cut == 0) unsup("unknown cutoff function");
       if (b.alpha < 1 || b.alpha > 8) unsup("angular power alpha outside 1..8");
       a.n = n;
       a.off = pot.ninR[I] + pot.offA[I][q];
       a.cut = b.cut;
+      a.phi = b.phi;
+      if (b.phi != ANG_GAUSS) P.gen = 1;
       a.alpha = b.alpha;
       a.rc = (float)b.rc;
       a.pirc = (float)(kPi / b.rc);
@@ -282,10 +284,11 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
       }
       a.nz = nz;
       // zeta <= 4 with |lambda| <= 1: ((1 + lambda cos)/2)^zeta is a polynomial of degree <= 4
-      // in cos with a non-negative base, which the moment-tensor path evaluates
+      // in cos with a non-negative base, which the moment-tensor path evaluates when the radial
+      // factor is a product h(r_ij) h(r_ik)
       bool lam_ok = true;
       for (int l = 0; l < a.nl; ++l) lam_ok = lam_ok && std::fabs((double)lams[l]) <= 1.0;
-      if ((1 << (nz - 1)) <= MOM_N && lam_ok) {
+      if ((1 << (nz - 1)) <= MOM_N && lam_ok && !ang_sum_family(b.phi)) {
         int J = 0, K = 0;
         for (int x = 0; x < pot.ntypes; ++x)
           for (int y = x; y < pot.ntypes; ++y)
@@ -295,6 +298,7 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
         moff += (J == K ? 1 : 2) * a.ne * MOM_C;
       } else {
         nz_max = std::max(nz_max, nz);  // the triplet kernels' zeta chain covers triplet blocks only
+        if (b.phi == ANG_IPOWP || b.phi == ANG_SECHP) P.kx = 1;
       }
       ne_max = std::max(ne_max, a.ne);
     }

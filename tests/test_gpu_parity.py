@@ -334,15 +334,19 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
         eng.close()
 
 
-@pytest.mark.parametrize("family", ["TANH", "SOFTPLUS", "LOGCOSH", "SWISH", "MISH"])
-def test_radial_families_against_oracle(native_lib, oracle_lib, tmp_path, family):
-    """Every radial family of BasisR (basis_radial.cpp:302-444) on the GPU against the oracle:
-    descriptors, energies and forces (the force terms follow the reference's expressions)."""
+@pytest.mark.parametrize("kind,family", [("radial", f) for f in ("TANH", "SOFTPLUS", "LOGCOSH", "SWISH", "MISH")] +
+                         [("angular", f) for f in ("IPOWP", "IPOWS", "SECHP", "SECHS")])
+def test_basis_families_against_oracle(native_lib, oracle_lib, tmp_path, kind, family):
+    """Every radial family of BasisR (basis_radial.cpp:302-444) and angular family of BasisA
+    (basis_angular.cpp:406-640) on the GPU against the oracle: descriptors, energies and forces
+    (the force terms follow the reference's expressions).  In the angular case the A-A blocks
+    (zeta up to 16) take the triplet path and the others, for the product families IPOWP and
+    SECHP, the moment path; the sum families IPOWS and SECHS take the triplet path throughout."""
     from atomnn_gb300 import engine
     pot = W.make_potential("mixed512")
-    for key, b in pot.radial.items():
+    for b in (pot.radial if kind == "radial" else pot.angular).values():
         b.phi = family
-    path = str(tmp_path / "radial.nnp")
+    path = str(tmp_path / "family.nnp")
     W.write_potential(pot, path)
     # networks scaled by the inputs' actual means for this family (taken from the oracle)
     orc = oracle_lib.OracleNNP(path)

@@ -108,6 +108,32 @@ def test_forces_match_finite_differences(oracle_lib, pot_mixed):
         assert abs(fd - F[atom, x]) < 1e-6 * max(1.0, abs(F[atom, x]))
 
 
+@pytest.mark.parametrize("kind,family", [("radial", f) for f in ("TANH", "SOFTPLUS", "LOGCOSH", "SWISH", "MISH")] +
+                         [("angular", f) for f in ("IPOWP", "IPOWS", "SECHP", "SECHS")])
+def test_basis_families_match_finite_differences(oracle_lib, tmp_path, kind, family):
+    """The force expressions of every radial (basis_radial.cpp:371-444) and angular
+    (basis_angular.cpp:456-640) family are the gradient of the energy they give, the property the
+    reference's test_basis_radial.cpp and test_basis_angular.cpp check by finite differences."""
+    pot = W.make_potential("mixed512")
+    for b in (pot.radial if kind == "radial" else pot.angular).values():
+        b.phi = family
+    path = str(tmp_path / "family.nnp")
+    W.write_potential(pot, path)
+    s = _big_cell()
+    orc = oracle_lib.OracleNNP(path)
+    _, F, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+    assert np.abs(F).max() > 1e-3
+    h = 1e-5
+    for atom, x in [(5, 1), (150, 0)]:
+        p = s.posn.copy()
+        p[atom, x] += h
+        ep, _, _ = orc.compute(p, s.species, s.cell, force=False)
+        p[atom, x] -= 2 * h
+        em, _, _ = orc.compute(p, s.species, s.cell, force=False)
+        fd = -(ep - em) / (2 * h)
+        assert abs(fd - F[atom, x]) < 1e-6 * max(1.0, abs(F[atom, x]))
+
+
 def test_min_image_quirk(oracle_lib, pot_small64, pot_mixed):
     """NNP::force adds the neighbour-side term only for the minimum image
     (src/nnp/nnp.cpp:445,471,475): forces of a cell narrower than 2 rc do not sum to zero,
