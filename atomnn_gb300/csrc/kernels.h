@@ -75,6 +75,8 @@ size_t force_smem_bytes(int cap, int ne, int warps, bool kx);
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st);
 size_t type_sort_ints(int natoms);  // ints of the type_count buffer for a batch of natoms
 void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile, cudaStream_t st);
+// stored FP64 descriptors (sstride per atom) into B.G (nin[t] values of each atom's type t)
+void launch_symm_load(const BatchDev& B, const int* nin, int ntypes, const double* src, int sstride, cudaStream_t st);
 int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weights, int ntypes, cudaStream_t st, const void* tcnets_host,
                         int want_grad);
 // the energy trainer's batch error and parameter gradient after a batched energy pass

@@ -96,6 +96,35 @@ __global__ void __launch_bounds__(256) type_scatter_kernel(int a0, int natoms, i
   }
 }
 
+// Stored descriptors (FP64 rows of sstride values) into the FP32 input rows of the networks:
+// atom i keeps its type's nin values, the rest of the row is zero.  Species outside the
+// potential are flagged in the status word.
+struct NinP {
+  int nin[NT_MAX];
+};
+__global__ void symm_load_kernel(int natoms, int ntypes, const NinP n, const int* __restrict__ type, const double* __restrict__ src,
+                                 int sstride, float* __restrict__ G, int gstride, int* __restrict__ status) {
+  const size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= (size_t)natoms * gstride) return;
+  const int i = (int)(w / gstride), k = (int)(w % gstride);
+  const int t = type[i];
+  if (t < 0 || t >= ntypes) {
+    if (k == 0) atomicOr(&status[ST_ERROR], ERR_BAD_TYPE);
+    G[w] = 0.f;
+    return;
+  }
+  G[w] = k < n.nin[t] ? (float)src[(size_t)i * sstride + k] : 0.f;
+}
+
+void launch_symm_load(const BatchDev& B, const int* nin, int ntypes, const double* src, int sstride, cudaStream_t st) {
+  if (B.natoms == 0) return;
+  NinP n{};
+  for (int t = 0; t < ntypes && t < NT_MAX; ++t) n.nin[t] = nin[t];
+  const size_t total = (size_t)B.natoms * B.gstride;
+  symm_load_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(B.natoms, ntypes, n, B.type + B.a0, src, sstride, B.G + (size_t)B.a0 * B.gstride,
+                                                                     B.gstride, B.status);
+}
+
 size_t type_sort_ints(int natoms) { return TC_BLK + 2 * (size_t)((natoms + 255) / 256) * NT_MAX; }
 
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st) {

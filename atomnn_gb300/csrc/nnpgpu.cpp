@@ -587,7 +587,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
                     &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
-                    &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad};
+                    &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);
@@ -976,6 +976,56 @@ extern "C" int nnpgpu_train_grad(nnpgpu_ctx* c, int nstruc, const int* natoms, c
   cudaMemcpyAsync(grad, c->tr_grad.p, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
   const cudaError_t err = cudaStreamSynchronize(st);
   if (err != cudaSuccess) return cuda_fail(c, err, "train");
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_energy_symm(nnpgpu_ctx* c, int nstruc, const int* natoms, const int* species, const double* symm, int symm_stride,
+                                  int flags, double* energy) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  cudaSetDevice(c->device);
+  if (nstruc < 0 || (nstruc > 0 && (!natoms || !energy))) return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: invalid batch description");
+  if (flags & ~(NNPGPU_BF16 | NNPGPU_NO_VACUUM))
+    return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: only NNPGPU_BF16 and NNPGPU_NO_VACUUM apply");
+  if (symm_stride < c->max_nin) return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: symm_stride below the largest input size");
+  size_t total = 0;
+  for (int s = 0; s < nstruc; ++s) {
+    if (natoms[s] < 0) return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: negative atom count");
+    total += (size_t)natoms[s];
+  }
+  if (total > 0 && (!species || !symm)) return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: species or descriptors missing");
+  for (size_t a = 0; a < total; ++a)
+    if (species[a] < 0 || species[a] >= c->pot.ntypes) return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: species index out of range");
+  if (nstruc == 0) return NNPGPU_OK;
+  cudaStream_t st = c->stream;
+  // no geometry: every structure is described as non-periodic, which only sets its atom range
+  const std::vector<double> no_cell(9 * (size_t)nstruc, 0.0);
+  Uploaded U;
+  int rc = prepare(c, nstruc, natoms, no_cell.data(), 32, U, st);
+  if (rc != NNPGPU_OK) return rc;
+  if (!ensure(c, c->symm_in, sizeof(double) * std::max<size_t>(total, 1) * symm_stride))
+    return set_error(c, NNPGPU_ERR_OOM, "energy_symm: device allocation failed or HBM budget exceeded");
+  cudaMemcpyAsync(c->type.p, species, sizeof(int) * total, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->symm_in.p, symm, sizeof(double) * total * symm_stride, cudaMemcpyHostToDevice, st);
+  BatchDev B = batch_view(c, U, (const double*)c->posn.p, (const int*)c->type.p, (double*)c->energy.p, (double*)c->force.p);
+  launch_symm_load(B, c->P.nin, c->pot.ntypes, (const double*)c->symm_in.p, symm_stride, st);
+  launch_type_sort(B, c->pot.ntypes, st);
+  if (flags & NNPGPU_BF16) {
+    const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st, c->tcnets ? c->tcnets->data() : nullptr, 0);
+    if (rcode == -1) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "BF16 network path unavailable for this potential");
+    if (rcode != 0) return cuda_fail(c, cudaGetLastError(), "tensor-core network set-up");
+  } else {
+    launch_network_fp32(B, c->nets, c->pot.ntypes, c->tune.nn_tile, st);
+  }
+  launch_gather(B, c->nets, !(flags & NNPGPU_NO_VACUUM), false, st);
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) return cuda_fail(c, le, "energy_symm launch");
+  int hstat[ST_WORDS];
+  cudaMemcpyAsync(energy, c->energy.p, sizeof(double) * nstruc, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(hstat, c->status.p, sizeof(hstat), cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(c, e, "energy_symm");
+  if (hstat[ST_ERROR] & ERR_BAD_TYPE) return set_error(c, NNPGPU_ERR_INVALID, "energy_symm: species index out of range");
   return NNPGPU_OK;
 }
 

@@ -19,7 +19,7 @@ EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntype
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
            "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
-           "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad"]
+           "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad", "nnpgpu_energy_symm"]
 
 _lib = None
 
@@ -72,6 +72,7 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_md_state.argtypes = [vp, vp, vp, vp, vp]
     L.nnpgpu_nparams.argtypes = [vp, ip]
     L.nnpgpu_train_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, ip, dp, vp, vp]
+    L.nnpgpu_energy_symm.argtypes = [vp, ip, vp, vp, vp, ip, ip, vp]
     L.nnpgpu_md_destroy.argtypes = [vp]
     L.nnpgpu_md_destroy.restype = None
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
@@ -206,6 +207,18 @@ class Engine:
         self._check(self.lib.nnpgpu_train_grad(self._ctx, len(structures), _p(natoms), _p(posn), _p(species), _p(cell), _p(eref),
                                                self.LOSS[loss], float(delta), _p(err), _p(grad)))
         return err[0], err[1], grad
+
+    def energy_symm(self, natoms, species, symm, flags=0):
+        """Energies of structures from stored descriptors (nnpgpu_energy_symm): natoms per
+        structure, species and symm rows (FP64, at least the largest input size wide) of all
+        their atoms concatenated."""
+        natoms = np.ascontiguousarray(natoms, dtype=np.int32)
+        species = np.ascontiguousarray(species, dtype=np.int32)
+        symm = np.ascontiguousarray(symm, dtype=np.float64)
+        energy = np.zeros(len(natoms))
+        self._check(self.lib.nnpgpu_energy_symm(self._ctx, len(natoms), _p(natoms), _p(species), _p(symm), symm.shape[1], int(flags),
+                                                _p(energy)))
+        return energy
 
     # ---- molecular dynamics on resident device state
     def md(self, struc, mass, dt, skin=1.0, vel=None, flags=0):

@@ -81,9 +81,12 @@ int max_input(const NNP& nnp) {
 }  // namespace
 
 // ------------------------------------------------------------------------------ Structure
-void Structure::resize(int nAtoms) {
+void Structure::resize(int nAtoms) { resize(nAtoms, atomT_); }
+
+void Structure::resize(int nAtoms, const AtomType& atomT) {
   if (nAtoms < 0) throw std::invalid_argument("Structure::resize: negative atom count");
   nAtoms_ = nAtoms;
+  atomT_ = atomT;
   name_.resize(nAtoms);
   type_.resize(nAtoms, -1);
   index_.resize(nAtoms);
@@ -91,6 +94,17 @@ void Structure::resize(int nAtoms) {
   posn_.resize(nAtoms);
   force_.resize(nAtoms);
   symm_.resize(nAtoms);
+  auto opt = [&](auto& v, bool on) { v.resize(on ? nAtoms : 0); };
+  opt(an_, atomT.an);
+  opt(mass_, atomT.mass);
+  opt(charge_, atomT.charge);
+  opt(radius_, atomT.radius);
+  opt(chi_, atomT.chi);
+  opt(eta_, atomT.eta);
+  opt(c6_, atomT.c6);
+  opt(js_, atomT.js);
+  opt(vel_, atomT.vel);
+  opt(spin_, atomT.spin);
 }
 
 void Structure::clear() {
@@ -107,6 +121,181 @@ bool Structure::periodic() const {
   return false;
 }
 
+// ------------------------------------------------------------------------------ binary files
+// The byte layout of serialize::pack for Structure (src/struc/structure.cpp:604-649, its parts in
+// src/struc/cell.cpp:182-206, src/struc/state.cpp:48-103, src/struc/atom_type.cpp:95-180,
+// src/mem/serialize.cpp:21-180 and src/math/eigen.cpp:40-160), native byte order:
+//   Cell      R, 9 doubles column-major
+//   State     energy ewald temp press qtot pe ke dt (doubles), t (int)
+//   AtomData  16 one-byte flags (name an type index mass charge radius chi eta c6 js posn vel
+//             force spin symm), int natoms, then each flagged property in that order:
+//             strings as int count + (int length + chars) each, int/double arrays as int count +
+//             values, 3-vectors as int count + 3 doubles each, symm as int count + (int size +
+//             doubles) per atom.
+// A file is an int byte count followed by those bytes.
+struct BinaryIO {
+  std::vector<char> buf;
+  size_t pos = 0;
+
+  template <class T>
+  void put(const T& v) {
+    const char* b = reinterpret_cast<const char*>(&v);
+    buf.insert(buf.end(), b, b + sizeof(T));
+  }
+  void put_bytes(const void* p, size_t n) {
+    const char* b = static_cast<const char*>(p);
+    buf.insert(buf.end(), b, b + n);
+  }
+  template <class T>
+  void put_vec(const std::vector<T>& v) {
+    put((int)v.size());
+    if (!v.empty()) put_bytes(v.data(), sizeof(T) * v.size());
+  }
+  void put_vec3(const std::vector<Vec3d>& v) {
+    put((int)v.size());
+    for (const Vec3d& x : v) put_bytes(x.data(), 3 * sizeof(double));
+  }
+  template <class T>
+  T get() {
+    T v;
+    get_bytes(&v, sizeof(T));
+    return v;
+  }
+  void get_bytes(void* p, size_t n) {
+    if (n > buf.size() - pos) throw std::runtime_error("read_binary: file ends inside a record");
+    std::memcpy(p, buf.data() + pos, n);
+    pos += n;
+  }
+  int get_count(size_t elem) {
+    const int n = get<int>();
+    if (n < 0 || (elem > 0 && (size_t)n > (buf.size() - pos) / elem)) throw std::runtime_error("read_binary: invalid element count");
+    return n;
+  }
+  template <class T>
+  void get_vec(std::vector<T>& v) {
+    v.resize(get_count(sizeof(T)));
+    if (!v.empty()) get_bytes(v.data(), sizeof(T) * v.size());
+  }
+  void get_vec3(std::vector<Vec3d>& v) {
+    v.resize(get_count(3 * sizeof(double)));
+    for (Vec3d& x : v) get_bytes(x.data(), 3 * sizeof(double));
+  }
+
+  static void pack(const Structure& s, BinaryIO& o) {
+    o.put_bytes(s.R_.data(), 9 * sizeof(double));
+    for (double v : {s.energy_, s.ewald_, s.temp_, s.press_, s.qtot_, s.pe_, s.ke_, s.dt_}) o.put(v);
+    o.put(s.t_);
+    const AtomType& a = s.atomT_;
+    for (bool f : {a.name, a.an, a.type, a.index, a.mass, a.charge, a.radius, a.chi, a.eta, a.c6, a.js, a.posn, a.vel, a.force, a.spin, a.symm})
+      o.put((char)(f ? 1 : 0));
+    o.put(s.nAtoms_);
+    if (a.name) {
+      o.put((int)s.name_.size());
+      for (const std::string& n : s.name_) {
+        o.put((int)n.size());
+        o.put_bytes(n.data(), n.size());
+      }
+    }
+    if (a.an) o.put_vec(s.an_);
+    if (a.type) o.put_vec(s.type_);
+    if (a.index) o.put_vec(s.index_);
+    if (a.mass) o.put_vec(s.mass_);
+    if (a.charge) o.put_vec(s.charge_);
+    if (a.radius) o.put_vec(s.radius_);
+    if (a.chi) o.put_vec(s.chi_);
+    if (a.eta) o.put_vec(s.eta_);
+    if (a.c6) o.put_vec(s.c6_);
+    if (a.js) o.put_vec(s.js_);
+    if (a.posn) o.put_vec3(s.posn_);
+    if (a.vel) o.put_vec3(s.vel_);
+    if (a.force) o.put_vec3(s.force_);
+    if (a.spin) o.put_vec3(s.spin_);
+    if (a.symm) {
+      o.put((int)s.symm_.size());
+      for (const std::vector<double>& g : s.symm_) o.put_vec(g);
+    }
+  }
+
+  static void unpack(Structure& s, BinaryIO& in) {
+    std::array<double, 9> R;
+    in.get_bytes(R.data(), 9 * sizeof(double));
+    double st[8];
+    for (double& v : st) v = in.get<double>();
+    const int t = in.get<int>();
+    AtomType a;
+    bool* flags[16] = {&a.name, &a.an, &a.type, &a.index, &a.mass, &a.charge, &a.radius, &a.chi,
+                       &a.eta, &a.c6, &a.js, &a.posn, &a.vel, &a.force, &a.spin, &a.symm};
+    for (bool* f : flags) *f = in.get<char>() != 0;
+    const int n = in.get<int>();
+    if (n < 0) throw std::runtime_error("read_binary: negative atom count");
+    Structure r;
+    r.resize(n, a);
+    r.R_ = R;
+    r.energy_ = st[0]; r.ewald_ = st[1]; r.temp_ = st[2]; r.press_ = st[3];
+    r.qtot_ = st[4]; r.pe_ = st[5]; r.ke_ = st[6]; r.dt_ = st[7];
+    r.t_ = t;
+    // each array must hold one entry per atom (AtomData::resize sizes them so in the reference)
+    auto need = [n](size_t got) {
+      if ((int)got != n) throw std::runtime_error("read_binary: per-atom array does not match the atom count");
+    };
+    if (a.name) {
+      r.name_.resize(in.get_count(sizeof(int)));
+      need(r.name_.size());
+      for (std::string& nm : r.name_) {
+        nm.resize(in.get_count(1));
+        if (!nm.empty()) in.get_bytes(&nm[0], nm.size());
+      }
+    }
+    if (a.an) { in.get_vec(r.an_); need(r.an_.size()); }
+    if (a.type) { in.get_vec(r.type_); need(r.type_.size()); }
+    if (a.index) { in.get_vec(r.index_); need(r.index_.size()); }
+    if (a.mass) { in.get_vec(r.mass_); need(r.mass_.size()); }
+    if (a.charge) { in.get_vec(r.charge_); need(r.charge_.size()); }
+    if (a.radius) { in.get_vec(r.radius_); need(r.radius_.size()); }
+    if (a.chi) { in.get_vec(r.chi_); need(r.chi_.size()); }
+    if (a.eta) { in.get_vec(r.eta_); need(r.eta_.size()); }
+    if (a.c6) { in.get_vec(r.c6_); need(r.c6_.size()); }
+    if (a.js) { in.get_vec(r.js_); need(r.js_.size()); }
+    if (a.posn) { in.get_vec3(r.posn_); need(r.posn_.size()); }
+    if (a.vel) { in.get_vec3(r.vel_); need(r.vel_.size()); }
+    if (a.force) { in.get_vec3(r.force_); need(r.force_.size()); }
+    if (a.spin) { in.get_vec3(r.spin_); need(r.spin_.size()); }
+    if (a.symm) {
+      r.symm_.resize(in.get_count(sizeof(int)));
+      need(r.symm_.size());
+      for (std::vector<double>& g : r.symm_) in.get_vec(g);
+    }
+    if (in.pos != in.buf.size()) throw std::runtime_error("read_binary: trailing bytes after the structure");
+    s = std::move(r);
+  }
+};
+
+void Structure::write_binary(const Structure& struc, const char* file) {
+  BinaryIO o;
+  BinaryIO::pack(struc, o);
+  std::FILE* f = std::fopen(file, "wb");
+  if (!f) throw std::runtime_error(std::string("write_binary(Structure&,const char*): Could not open file: ") + file);
+  const int nbytes = (int)o.buf.size();
+  const bool ok = std::fwrite(&nbytes, sizeof(int), 1, f) == 1 && std::fwrite(o.buf.data(), 1, o.buf.size(), f) == o.buf.size();
+  const bool closed = std::fclose(f) == 0;
+  if (!ok || !closed) throw std::runtime_error(std::string("write_binary(Structure&,const char*): Write error: ") + file);
+}
+
+void Structure::read_binary(Structure& struc, const char* file) {
+  std::FILE* f = std::fopen(file, "rb");
+  if (!f) throw std::runtime_error(std::string("read_binary(Structure&,const char*): Could not open file: ") + file);
+  BinaryIO in;
+  int nbytes = 0;
+  bool ok = std::fread(&nbytes, sizeof(int), 1, f) == 1 && nbytes >= 0;
+  if (ok) {
+    in.buf.resize((size_t)nbytes);
+    ok = std::fread(in.buf.data(), 1, in.buf.size(), f) == in.buf.size();
+  }
+  std::fclose(f);
+  if (!ok) throw std::runtime_error(std::string("read_binary(Structure&,const char*): Read error: ") + file);
+  BinaryIO::unpack(struc, in);
+}
+
 // ------------------------------------------------------------------------------ NNP
 int NNP::ntypes() const { return ctx_ ? nnpgpu_ntypes(ctx_.get()) : 0; }
 int NNP::index(const char* name) const { return ctx_ ? nnpgpu_type_index(ctx_.get(), name) : -1; }
@@ -121,26 +310,8 @@ void NNP::read(const char* file, NNP& nnp, const nnpgpu_opts* opts) {
   if (code != NNPGPU_OK) fail(c, code, "NNP::read");
   nnp.ctx_ = holder;
   nnp.file_ = file;
-  nnp.cached_ = false;
   std::lock_guard<std::mutex> l(g_last_mu);
   g_last = holder;
-}
-
-uint64_t NNP::fingerprint(const Structure& struc) {
-  // FNV-1a over atom count, lattice, types and positions
-  uint64_t h = 1469598103934665603ull;
-  auto mix = [&](const void* p, size_t n) {
-    const unsigned char* b = (const unsigned char*)p;
-    for (size_t k = 0; k < n; ++k) h = (h ^ b[k]) * 1099511628211ull;
-  };
-  const int n = struc.nAtoms();
-  mix(&n, sizeof(n));
-  mix(struc.R().data(), sizeof(double) * 9);
-  if (n > 0) {
-    mix(struc.type().data(), sizeof(int) * n);
-    mix(struc.posn().data(), sizeof(Vec3d) * n);
-  }
-  return h;
 }
 
 void NNP::init(const NNP& nnp, Structure& struc) {
@@ -158,25 +329,34 @@ void NNP::symm(NNP& nnp, Structure& struc, const NeighborList&) {
   flatten(nnp, &p, 1, f);
   const int stride = max_input(nnp);
   std::vector<float> G((size_t)std::max(struc.nAtoms(), 1) * stride);
-  double e = 0.0;
-  const int flags = NNPGPU_SYMM | NNPGPU_ENERGY | (nnp.bf16_ ? NNPGPU_BF16 : 0);
-  check(nnp.ctx(), nnpgpu_compute(nnp.ctx(), 1, f.natoms.data(), f.posn.data(), f.species.data(), f.cell.data(), flags, &e, nullptr, G.data()),
+  check(nnp.ctx(), nnpgpu_compute(nnp.ctx(), 1, f.natoms.data(), f.posn.data(), f.species.data(), f.cell.data(), NNPGPU_SYMM, nullptr,
+                                  nullptr, G.data()),
         "NNP::symm");
   for (int i = 0; i < struc.nAtoms(); ++i) {
     const int nin = nnp.nInput(struc.type(i));
     struc.symm(i).resize(nin);
     for (int k = 0; k < nin; ++k) struc.symm(i)[k] = G[(size_t)i * stride + k];
   }
-  nnp.cached_key_ = fingerprint(struc);
-  nnp.cached_energy_ = e;
-  nnp.cached_ = true;
 }
 
 double NNP::energy(NNP& nnp, Structure& struc) {
   if (!nnp.ctx_) throw std::runtime_error("NNP::energy: no potential read");
-  if (nnp.cached_ && nnp.cached_key_ == fingerprint(struc)) {
-    struc.energy() = nnp.cached_energy_;
-    return struc.energy();
+  const int n = struc.nAtoms();
+  bool filled = n > 0;
+  for (int i = 0; i < n && filled; ++i) {
+    const int t = struc.type(i);
+    if (t < 0 || t >= nnp.ntypes()) throw std::invalid_argument("NNP::energy: atom type not in the potential");
+    filled = (int)struc.symm(i).size() == nnp.nInput(t);
+  }
+  if (filled) {  // the reference's path: the networks on the stored descriptors
+    const int stride = max_input(nnp);
+    std::vector<double> G((size_t)n * stride, 0.0);
+    for (int i = 0; i < n; ++i) std::copy(struc.symm(i).begin(), struc.symm(i).end(), G.begin() + (size_t)i * stride);
+    double e = 0.0;
+    check(nnp.ctx(), nnpgpu_energy_symm(nnp.ctx(), 1, &n, struc.type().data(), G.data(), stride, nnp.bf16_ ? NNPGPU_BF16 : 0, &e),
+          "NNP::energy");
+    struc.energy() = e;
+    return e;
   }
   const Structure* p = &struc;
   Flat f;

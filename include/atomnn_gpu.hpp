@@ -3,7 +3,9 @@
 // The classes keep the names and call shapes of the reference's hot-path API so that a caller
 // changes its includes and a using-declaration, not its calls:
 //   NNP::read / init / symm / energy / force / compute   src/nnp/nnp.hpp:108-120
-//   Structure (AtomData + Cell + State subset)           src/struc/structure.hpp:38-178
+//   Structure (AtomData + Cell + State), AtomType        src/struc/structure.hpp:38-178,
+//                                                        src/struc/atom_type.hpp:14-50
+//   Structure::write_binary / read_binary                src/struc/structure.cpp:117-190
 //   NeighborList::build, Neighbor                        src/struc/neighbor.hpp:28-85
 //   VASP::POSCAR::read, XYZ::read                        src/format/vasp_struc.cpp:51-200,
 //                                                        src/format/xyz_struc.cpp:38-130
@@ -16,9 +18,9 @@
 //  * NNP::symm/energy/force/compute take the NeighborList argument for signature parity; the
 //    GPU builds its own list at nnp.rc() (the same list NeighborList::build gives at that
 //    cutoff).
-//  * NNP::energy evaluates the networks on descriptors the GPU computes from the positions, not
-//    on whatever the caller stored in struc.symm().  NNP::symm fills struc.symm() and keeps the
-//    energy of the same positions, so symm followed by energy costs one evaluation.
+//  * NNP::energy evaluates the networks on struc.symm() as the reference does, when every atom
+//    holds a descriptor row of its type's input size (after NNP::symm, or read back from a
+//    binary structure file); otherwise it computes the descriptors from the positions first.
 //  * NNP::compute(nnp, std::vector<Structure>&, ...) evaluates many structures in one batched
 //    launch sequence; it is the call the GPU is built for.
 #pragma once
@@ -47,15 +49,29 @@ struct Vec3d {
   const double* data() const { return v; }
 };
 
-// One structure: atom names, types, positions, forces, descriptors, the lattice and the energy.
+// Which per-atom properties a structure carries (AtomType, src/struc/atom_type.hpp:14-50).  name,
+// type, index, posn, force and symm are always allocated here; the flags say which of them a
+// binary structure file holds, and which of the other properties are allocated.
+struct AtomType {
+  bool frac = false;
+  bool name = true, an = false, type = true, index = true;
+  bool mass = false, charge = false, radius = false, chi = false, eta = false, c6 = false, js = false;
+  bool posn = true, vel = false, force = true, spin = false;
+  bool symm = true;
+};
+
+// One structure: per-atom data (AtomData), the lattice (Cell) and the scalar state (State).
 class Structure {
  public:
   Structure() = default;
   explicit Structure(int nAtoms) { resize(nAtoms); }
+  Structure(int nAtoms, const AtomType& atomT) { resize(nAtoms, atomT); }
 
   void resize(int nAtoms);
+  void resize(int nAtoms, const AtomType& atomT);
   void clear();
   int nAtoms() const { return nAtoms_; }
+  const AtomType& atomType() const { return atomT_; }
 
   // lattice (Cell::init, src/struc/cell.cpp:45-70): lv column-major, columns = lattice vectors;
   // an all-zero lattice means a non-periodic structure
@@ -90,18 +106,59 @@ class Structure {
   std::vector<double>& symm(int i) { return symm_[i]; }
   const std::vector<double>& symm(int i) const { return symm_[i]; }
 
-  // State
+  // properties allocated when the AtomType flag is set (empty otherwise)
+  std::vector<int>& an() { return an_; }
+  int& an(int i) { return an_[i]; }
+  std::vector<double>& mass() { return mass_; }
+  double& mass(int i) { return mass_[i]; }
+  std::vector<double>& charge() { return charge_; }
+  double& charge(int i) { return charge_[i]; }
+  std::vector<double>& radius() { return radius_; }
+  double& radius(int i) { return radius_[i]; }
+  std::vector<double>& chi() { return chi_; }
+  double& chi(int i) { return chi_[i]; }
+  std::vector<double>& eta() { return eta_; }
+  double& eta(int i) { return eta_[i]; }
+  std::vector<double>& c6() { return c6_; }
+  double& c6(int i) { return c6_[i]; }
+  std::vector<double>& js() { return js_; }
+  double& js(int i) { return js_[i]; }
+  std::vector<Vec3d>& vel() { return vel_; }
+  Vec3d& vel(int i) { return vel_[i]; }
+  std::vector<Vec3d>& spin() { return spin_; }
+  Vec3d& spin(int i) { return spin_[i]; }
+
+  // State (src/struc/state.hpp)
   double& energy() { return energy_; }
   const double& energy() const { return energy_; }
+  double& ewald() { return ewald_; }
+  double& temp() { return temp_; }
+  double& press() { return press_; }
+  double& qtot() { return qtot_; }
+  double& pe() { return pe_; }
+  double& ke() { return ke_; }
+  double& dt() { return dt_; }
+  int& t() { return t_; }
+
+  // Structure::write_binary / read_binary (src/struc/structure.cpp:117-190): the reference's
+  // byte layout (an int byte count, then the lattice, the state and the per-atom data the
+  // AtomType flags select), so files pass between the two codes.  Throw std::runtime_error on
+  // IO errors and on a malformed file.
+  static void write_binary(const Structure& struc, const char* file);
+  static void read_binary(Structure& struc, const char* file);
 
  private:
+  friend struct BinaryIO;
   int nAtoms_ = 0;
+  AtomType atomT_;
   std::array<double, 9> R_{};
   std::vector<std::string> name_;
-  std::vector<int> type_, index_;
-  std::vector<Vec3d> posn_, force_;
+  std::vector<int> type_, index_, an_;
+  std::vector<double> mass_, charge_, radius_, chi_, eta_, c6_, js_;
+  std::vector<Vec3d> posn_, force_, vel_, spin_;
   std::vector<std::vector<double>> symm_;
-  double energy_ = 0.0;
+  double energy_ = 0.0, ewald_ = 0.0, temp_ = 0.0, press_ = 0.0, qtot_ = 0.0, pe_ = 0.0, ke_ = 0.0, dt_ = 0.0;
+  int t_ = 0;
 };
 
 // One entry of a neighbour list (Neighbor, src/struc/neighbor.hpp:28-54): r points from the
@@ -173,8 +230,9 @@ class NNP {
   static void init(const NNP& nnp, Structure& struc);
   // NNP::symm: struc.symm(i) for every atom (nnp.cpp:334-381)
   static void symm(NNP& nnp, Structure& struc, const NeighborList& nlist);
-  // NNP::energy: sum of atomic energies including each species' vacuum energy (nnp.cpp:390-402);
-  // sets struc.energy() and returns it
+  // NNP::energy: sum of atomic energies including each species' vacuum energy (nnp.cpp:390-402),
+  // the networks evaluated on struc.symm() (from the positions when symm is not filled); sets
+  // struc.energy() and returns it
   static double energy(NNP& nnp, Structure& struc);
   // NNP::force: struc.force(i) (nnp.cpp:416-482)
   static void force(NNP& nnp, Structure& struc, const NeighborList& nlist);
@@ -189,11 +247,6 @@ class NNP {
   std::shared_ptr<nnpgpu_ctx> ctx_;
   std::string file_;
   bool bf16_ = false;
-  // energy of the last NNP::symm call, valid for the positions it was computed from
-  uint64_t cached_key_ = 0;
-  double cached_energy_ = 0.0;
-  bool cached_ = false;
-  static uint64_t fingerprint(const Structure& struc);
   friend class NeighborList;
 };
 

@@ -120,6 +120,16 @@ int nnpgpu_profile_enable(nnpgpu_ctx* ctx, int on);
 int nnpgpu_profile_read(const nnpgpu_ctx* ctx, int stage, double* total_ms, long long* count);
 const char* nnpgpu_profile_stage_name(int stage);
 
+/* ---- energies from stored descriptors: NNP::energy on struc.symm() (src/nnp/nnp.cpp:390-402, the
+ * network pass ANN::fp of src/ml/nn.cpp:1191-1209), as the trainers use it on descriptors read
+ * back from a binary structure file (Structure::read_binary, src/struc/structure.cpp:155-190).
+ * No neighbour list and no descriptor pass: symm[sum(natoms)][symm_stride] (FP64, row-major;
+ * atom i's first nnpgpu_ninput(ctx, species[i]) values are used, symm_stride >= every input
+ * size); flags: NNPGPU_BF16, NNPGPU_NO_VACUUM; energy[nstruc] (FP64).  The networks run in FP32
+ * (or BF16) on the descriptors rounded to FP32. */
+int nnpgpu_energy_symm(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const int* species, const double* symm,
+                       int symm_stride, int flags, double* energy);
+
 /* ---- training: the energy trainer's batch error and parameter gradient.  Replaces the error and
  * gradient part of NNPTE::error (src/nnp/nnpte.cpp:870-921) with Cost::grad (src/ml/nn.cpp:1554-1589):
  * per structure E = sum of the atomic network outputs (no vacuum energies), dE = (E - E_ref)/N and

@@ -2,9 +2,11 @@
 // compute tool drives AtomNN (src/nnp/nnpce.cpp:259-281) and prints every result, so that the
 // test can compare them with the oracle.
 //
-// usage: api_check <potential> <POSCAR>
+// usage: api_check <potential> <POSCAR> <scratch binary file>
 // prints: "nlist <atoms> <entries> <min entries>", "symm <i> <k> <value>" for atom 0,
-//         "energy <E>", "compute <E without vacuum>", "force <i> <fx> <fy> <fz>", "batched <E>"
+//         "energy <E>", "cached <E>" (the networks on descriptors written to and read back from
+//         a binary structure file), "positions <E>" (descriptors cleared: from the positions),
+//         "compute <E without vacuum>", "force <i> <fx> <fy> <fz>", "batched <E>"
 #include <cstdio>
 #include <exception>
 #include <vector>
@@ -14,7 +16,7 @@
 using namespace atomnn_gpu;
 
 int main(int argc, char** argv) {
-  if (argc < 3) return 2;
+  if (argc < 4) return 2;
   try {
     NNP nnp;
     NNP::read(argv[1], nnp);
@@ -35,6 +37,14 @@ int main(int argc, char** argv) {
     for (size_t k = 0; k < struc.symm(0).size(); ++k) std::printf("symm 0 %zu %.9e\n", k, struc.symm(0)[k]);
     const double e = NNP::energy(nnp, struc);
     std::printf("energy %.10f\n", e);
+    // the trainers' descriptor cache: the structure with its descriptors written to a binary
+    // file, read back and evaluated without a neighbour list
+    Structure::write_binary(struc, argv[3]);
+    Structure back;
+    Structure::read_binary(back, argv[3]);
+    std::printf("cached %.10f\n", NNP::energy(nnp, back));
+    for (int i = 0; i < back.nAtoms(); ++i) back.symm(i).clear();
+    std::printf("positions %.10f\n", NNP::energy(nnp, back));
     NNP::force(nnp, struc, nlist);
     for (int i = 0; i < struc.nAtoms(); ++i)
       std::printf("force %d %.10f %.10f %.10f\n", i, struc.force(i)[0], struc.force(i)[1], struc.force(i)[2]);

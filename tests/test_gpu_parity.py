@@ -334,6 +334,49 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
         eng.close()
 
 
+def test_energy_from_stored_descriptors(engines, oracles):
+    """nnpgpu_energy_symm: NNP::energy on stored descriptors (nnp.cpp:390-402), as the trainers
+    evaluate structures read back from binary files, on the oracle's FP64 descriptors.  With and
+    without the vacuum energies, FP32 and BF16 networks, one-atom and empty structures included."""
+    from atomnn_gb300 import engine
+    eng, orc = engines["mixed512"], oracles["mixed512"]
+    strucs = W.make_structures("mixed512", seed=41, count=4, sizes=[30, 300, 1500, 2])
+    strucs.insert(1, W.Structure(posn=np.zeros((1, 3)), species=np.array([1], np.int32), cell=np.zeros((3, 3))))
+    eo, rows = [], []
+    for s in strucs:
+        e, _, G = orc.compute(s.posn, s.species, s.cell, force=False, symm=True)
+        eo.append(e)
+        rows.append(G)
+    width = max(eng.ninput)
+    symm = np.zeros((sum(s.natoms for s in strucs), width + 3))  # wider rows than needed are fine
+    off = 0
+    for s, G in zip(strucs, rows):
+        symm[off:off + s.natoms, :G.shape[1]] = G
+        off += s.natoms
+    natoms = [s.natoms for s in strucs] + [0]
+    species = np.concatenate([s.species for s in strucs])
+    e = eng.energy_symm(natoms, species, symm)
+    e_nv = eng.energy_symm(natoms, species, symm, flags=engine.NO_VACUUM)
+    e_bf = eng.energy_symm(natoms, species, symm, flags=engine.BF16)
+    pot = W.make_potential("mixed512")
+    for k, s in enumerate(strucs):
+        assert abs(e[k] - eo[k]) / s.natoms <= E_TOL, (k, e[k], eo[k])
+        assert abs(e_bf[k] - eo[k]) / s.natoms <= BF16_E_TOL
+        evac = sum(pot.species[t].energy for t in s.species)
+        assert abs((e[k] - e_nv[k]) - evac) <= 1e-9 * max(1.0, abs(evac))
+    assert e[-1] == 0.0 and e_nv[-1] == 0.0
+    # the same structures through the positions give the same energies
+    ec, _, _ = eng.compute(strucs, _flags("ENERGY", "BATCHED"))
+    for k, s in enumerate(strucs):
+        assert abs(e[k] - ec[k]) / s.natoms <= E_TOL
+    with pytest.raises(engine.NNPGPUError):
+        eng.energy_symm(natoms, species, symm[:, :width - 1])
+    bad = species.copy()
+    bad[3] = 5
+    with pytest.raises(engine.NNPGPUError):
+        eng.energy_symm(natoms, bad, symm)
+
+
 @pytest.mark.parametrize("kind,family", [("radial", f) for f in ("TANH", "SOFTPLUS", "LOGCOSH", "SWISH", "MISH")] +
                          [("angular", f) for f in ("IPOWP", "IPOWS", "SECHP", "SECHS")])
 def test_basis_families_against_oracle(native_lib, oracle_lib, tmp_path, kind, family):

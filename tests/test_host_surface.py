@@ -119,6 +119,92 @@ def test_missing_structure_file(tool, tmp_path):
     assert rc == 1 and "Could not open" in out
 
 
+@pytest.fixture(scope="module")
+def binary_check(native_lib, tmp_path_factory):
+    from atomnn_gb300 import build
+    build.build_host()
+    exe = str(tmp_path_factory.mktemp("bin") / "binary_check")
+    out_dir = os.path.join(REPO, "atomnn_gb300", "_build")
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I" + os.path.join(REPO, "include"), os.path.join(REPO, "tests", "cpp", "binary_check.cpp"),
+                    "-o", exe, "-L" + out_dir, "-latomnn_gpu", "-lnnpgpu", "-Wl,-rpath," + out_dir], check=True)
+    return exe
+
+
+def _binary_struc(rng, natoms, flags):
+    from oracle import struc_binary as SB
+    s = {"R": rng.normal(size=(3, 3)), "natoms": natoms, "t": int(rng.integers(0, 1000)),
+         "flags": {f: (f in flags) for f in SB.FLAGS}}
+    for k in SB.STATE:
+        s[k] = float(rng.normal())
+    s["name"] = [["Mg", "O", "Xx_long_name"][k % 3] for k in range(natoms)]
+    for k in SB.INTS:
+        s[k] = rng.integers(-5, 100, natoms)
+    for k in SB.DOUBLES:
+        s[k] = rng.normal(size=natoms)
+    for k in SB.VEC3:
+        s[k] = rng.normal(size=(natoms, 3))
+    s["symm"] = [rng.normal(size=int(rng.integers(0, 9))) for _ in range(natoms)]
+    return s
+
+
+@pytest.mark.parametrize("flags", ["all", "default", "posn_only"])
+def test_binary_structure_roundtrip(binary_check, tmp_path, flags):
+    """Structure::read_binary of a file written by the layout's restatement (oracle/struc_binary.py)
+    gives every flagged property; Structure::write_binary writes the same bytes back."""
+    from oracle import struc_binary as SB
+    sel = {"all": SB.FLAGS, "default": ["name", "type", "index", "posn", "force", "symm"], "posn_only": ["posn"]}[flags]
+    rng = np.random.default_rng(len(flags))
+    s = _binary_struc(rng, 7, sel)
+    src, dst = tmp_path / "in.dat", tmp_path / "out.dat"
+    src.write_bytes(SB.pack(s))
+    rc, out = _run(binary_check, str(src), str(dst))
+    assert rc == 0, out
+    assert dst.read_bytes() == src.read_bytes()
+    rows = [l.split() for l in out.splitlines()]
+    assert rows[0] == ["natoms", "7"]
+    assert rows[1][1] == "".join("1" if f in sel else "0" for f in SB.FLAGS)
+    np.testing.assert_array_equal([float(x) for x in rows[2][1:]], s["R"].flatten(order="F"))
+    np.testing.assert_array_equal([float(x) for x in rows[3][1:9]], [s[k] for k in SB.STATE])
+    assert int(rows[3][9]) == s["t"]
+    atoms = [r for r in rows if r[0] == "atom"]
+    extra = [r for r in rows if r[0] == "extra"]
+    for i in range(7):
+        a, x = atoms[i], extra[i]
+        assert a[2] == (s["name"][i] if "name" in sel else "-")
+        assert int(a[3]) == (s["type"][i] if "type" in sel else -1)
+        assert int(a[4]) == (s["index"][i] if "index" in sel else i)
+        np.testing.assert_array_equal([float(v) for v in a[5:8]], s["posn"][i])
+        np.testing.assert_array_equal([float(v) for v in a[8:11]], s["force"][i] if "force" in sel else np.zeros(3))
+        g = s["symm"][i] if "symm" in sel else np.zeros(0)
+        total = 0.0
+        for v in g.tolist():  # summed in order, as the C++ side does (sum() compensates)
+            total += v
+        assert int(a[11]) == len(g) and float(a[12]) == total
+        assert int(x[2]) == (s["an"][i] if "an" in sel else 0)
+        for k, name in enumerate(SB.DOUBLES):
+            assert float(x[3 + k]) == (s[name][i] if name in sel else 0.0)
+        np.testing.assert_array_equal([float(v) for v in x[10:13]], s["vel"][i] if "vel" in sel else np.zeros(3))
+        np.testing.assert_array_equal([float(v) for v in x[13:16]], s["spin"][i] if "spin" in sel else np.zeros(3))
+
+
+def test_binary_structure_rejects_malformed(binary_check, tmp_path):
+    from oracle import struc_binary as SB
+    rng = np.random.default_rng(3)
+    good = SB.pack(_binary_struc(rng, 5, SB.FLAGS))
+    bad_files = {
+        "truncated": good[:-9],
+        "count_mismatch": good[:4] + good[4:4 + 72 + 64 + 4 + 16] + (6).to_bytes(4, "little") + good[4 + 72 + 64 + 4 + 16 + 4:],
+        "trailing": (len(good) - 4 + 3).to_bytes(4, "little") + good[4:] + b"abc",
+    }
+    for name, data in bad_files.items():
+        p = tmp_path / (name + ".dat")
+        p.write_bytes(data)
+        rc, out = _run(binary_check, str(p), str(tmp_path / "o.dat"))
+        assert rc == 1 and "ERROR" in out and "read_binary" in out, (name, out)
+    rc, out = _run(binary_check, str(tmp_path / "missing.dat"), str(tmp_path / "o.dat"))
+    assert rc == 1 and "Could not open" in out
+
+
 @pytest.mark.gpu
 def test_tool_matches_oracle(tool, tmp_path, oracle_lib):
     strucs = _structures()
@@ -156,7 +242,7 @@ def test_cpp_api_matches_oracle(native_lib, tmp_path, oracle_lib):
     s = _structures()[1]
     p = str(tmp_path / "POSCAR")
     _write_poscar(p, s)
-    rc, out = _run(exe, os.path.join(GOLDEN, "mixed512.nnp"), p)
+    rc, out = _run(exe, os.path.join(GOLDEN, "mixed512.nnp"), p, str(tmp_path / "struc.dat"))
     assert rc == 0, out
     rows = [l.split() for l in out.splitlines()]
     pot = os.path.join(GOLDEN, "mixed512.nnp")
@@ -172,6 +258,9 @@ def test_cpp_api_matches_oracle(native_lib, tmp_path, oracle_lib):
     np.testing.assert_allclose(G0, Go[0, :len(G0)], rtol=0, atol=1e-5 * scale)
     e = float([r for r in rows if r[0] == "energy"][0][1])
     assert abs(e - eo) / s.natoms <= E_TOL
+    # stored descriptors read back from the binary file give the same energy; so do the positions
+    assert float([r for r in rows if r[0] == "cached"][0][1]) == e
+    assert abs(float([r for r in rows if r[0] == "positions"][0][1]) - eo) / s.natoms <= E_TOL
     F = np.array([[float(x) for x in r[2:5]] for r in rows if r[0] == "force"])
     assert np.abs(F - Fo).max() <= F_TOL
     assert abs(float([r for r in rows if r[0] == "compute"][0][1]) - ec) / s.natoms <= E_TOL
