@@ -1071,6 +1071,187 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   for (int p = lane; p < n; p += 32) Wi[S.orig[p]] = make_float4(S.wx[p], S.wy[p], S.wz[p], 0.f);
 }
 
+// ------------------------------------------------------------------------------------ tangent
+// The force term of the force trainer's loss (loss of NNPTEF::error, src/nnp/nnptef.cpp:1043-1135)
+// reaches the network parameters through dE/dG: with t_k = dloss/dF_k, the descriptor-space
+// weights are u_if = sum_k t_k . dF_k/d(dE/dG_if), F as NNP::force builds it (nnp.cpp:416-482).
+// Per neighbour slot p of centre i, the neighbour's tangent counts only for the minimum image:
+// delta_p = t_i - (min_p ? t_j : 0).  Then for a radial function u_f = -sum_p dG_f/dr (delta_p . u_p)
+// and for an angular one u_f = -sum_triplets (dG_f/dcos dcos + dG_f/dr_a (delta_a . u_a) +
+// dG_f/dr_b (delta_b . u_b)), dcos = delta_a.(u_b - cos u_a)/r_a + delta_b.(u_a - cos u_b)/r_b:
+// minus the tangent of the descriptors along the masked displacement field.  Every angular block
+// takes the triplet loop here (moment blocks included), all families through ang_h.
+template <int NE, int NZ>
+__device__ void tangent_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  const int lane = threadIdx.x & 31;
+  float acc[NE][NL][NZ];
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) acc[e][l][m] = 0.f;
+  const bool sum = ang_sum_family(A.phi);
+  const float lam0 = A.lam[0], lam1 = A.lam[1];
+  for (int q = 0; q * 32 < sc.nown; ++q) {
+    const int x = q * 32 + lane;
+    const int a = sc.xb + min(x, sc.nown - 1);
+    const float uax = S.ux[a], uay = S.uy[a], uaz = S.uz[a], ia = S.inv[a];
+    const float dax = S.wx[a], day = S.wy[a], daz = S.wz[a];
+    const float fa = S.fc[a], ga = S.gc[a], pa = S.dpa[a];
+    const float dda = dax * uax + day * uay + daz * uaz;
+    for (int dd = sc.d0; dd <= sc.d1; ++dd) {
+      const int nx = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+      if (x < nx) {
+        int y = x + dd;
+        if (y >= sc.mod) y -= sc.mod;
+        const int b = sc.yb + y;
+        const float ubx = S.ux[b], uby = S.uy[b], ubz = S.uz[b], ib = S.inv[b];
+        const float dbx = S.wx[b], dby = S.wy[b], dbz = S.wz[b];
+        const float fb = S.fc[b], gb = S.gc[b], pb = S.dpa[b];
+        const float cs = uax * ubx + uay * uby + uaz * ubz;
+        const float ddb = dbx * ubx + dby * uby + dbz * ubz;
+        const float xa = dax * ubx + day * uby + daz * ubz, xb = dbx * uax + dby * uay + dbz * uaz;
+        const float dcos = (xa - cs * dda) * ia + (xb - cs * ddb) * ib;
+        float p[NL][NZ], qd[NL][NZ];
+        p[0][0] = fabsf(0.5f * (1.0f + lam0 * cs));
+        p[1][0] = fabsf(0.5f * (1.0f + lam1 * cs));
+#pragma unroll
+        for (int l = 0; l < NL; ++l) {
+          qd[l][0] = 1.0f;
+#pragma unroll
+          for (int m = 1; m < NZ; ++m) {
+            qd[l][m] = 2.0f * qd[l][m - 1] * p[l][m - 1];
+            p[l][m] = p[l][m - 1] * p[l][m - 1];
+          }
+        }
+#pragma unroll
+        for (int e = 0; e < NE; ++e) {
+          if (e >= A.ne) break;
+          float R, ka, kb;
+          if (sum) {
+            R = ang_h(A.phi, A.ietap[e] * (S.ex[a] + S.ex[b]), ka);
+            kb = ka;
+          } else {
+            R = S.ex[e * cap + a] * S.ex[e * cap + b];
+            ka = S.kx[e * cap + a];
+            kb = S.kx[e * cap + b];
+          }
+          const float ie = A.ietap[e];
+          const float td = R * (fb * (ga - ie * ka * pa) * dda + fa * (gb - ie * kb * pb) * ddb);
+          const float tc = 0.5f * fa * fb * R * dcos;
+          const float tc0 = lam0 * tc, tc1 = lam1 * tc;
+#pragma unroll
+          for (int m = 0; m < NZ; ++m) {
+            acc[e][0][m] = fmaf(qd[0][m], tc0, fmaf(p[0][m], td, acc[e][0][m]));
+            acc[e][1][m] = fmaf(qd[1][m], tc1, fmaf(p[1][m], td, acc[e][1][m]));
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < NE; ++e)
+#pragma unroll
+    for (int l = 0; l < NL; ++l)
+#pragma unroll
+      for (int m = 0; m < NZ; ++m) {
+        const float v = warp_sum(acc[e][l][m]);
+        if (lane == 0) S.scratch[(e * NL + l) * NZ_MAX + m] = v;
+      }
+}
+
+template <int NEK, int NZK>
+__global__ void __launch_bounds__(128) tangent_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
+                                                      const int* __restrict__ type, const int* __restrict__ nb_j,
+                                                      const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
+                                                      const int* __restrict__ nb_code, const int* __restrict__ nb_cnt,
+                                                      const float4* __restrict__ tvec, float* __restrict__ U, int gstride) {
+  extern __shared__ float smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
+  if (i >= a0 + natoms) return;
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, true), cap, NEK, true);
+  const int I = clamp_type(type[i], P.ntypes);
+  const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
+  const bool cc = cutoff_cache(S, P, I, n);
+  // masked displacement of each staged slot
+  const float4 ti = tvec[i];
+  for (int p = lane; p < n; p += 32) {
+    const size_t g = (size_t)i * cap + S.orig[p];
+    const bool mn = code_min(nb_code[g]);
+    const float4 tj = mn ? tvec[nb_j[g]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    S.wx[p] = ti.x - tj.x;
+    S.wy[p] = ti.y - tj.y;
+    S.wz[p] = ti.z - tj.z;
+  }
+  __syncwarp();
+  float* Ui = U + (size_t)i * gstride;
+  for (int k = P.nin[I] + lane; k < gstride; k += 32) Ui[k] = 0.f;
+
+  // radial: u_f = -norm sum_p dG_f/dr (delta_p . u_p), dG_f/dr per function as BasisR::force uses it
+  for (int J = 0; J < P.ntypes; ++J) {
+    const RadialP& R = P.rad[I][J];
+    const int p0 = S.toff[J], p1 = S.toff[J + 1];
+    for (int f0 = 0; f0 < R.n; f0 += 4) {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      for (int p = p0 + lane; p < p1; p += 32) {
+        const float d = S.d[p];
+        float fc, gc;
+        if (cc) { fc = S.fc[p]; gc = S.gc[p]; }
+        else cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
+        const float proj = S.wx[p] * S.ux[p] + S.wy[p] * S.uy[p] + S.wz[p] * S.uz[p];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (f0 + k < R.n) acc[k] = fmaf(radial_force_term(R.phi, R.eta[f0 + k], R.rs[f0 + k], d, fc, gc), proj, acc[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float v = warp_sum(acc[k]);
+        if (lane == 0 && f0 + k < R.n) Ui[R.off + f0 + k] = -v * R.norm;
+      }
+    }
+  }
+  __syncwarp();
+
+  // angular: every block through the triplet loop
+  for (int J = 0; J < P.ntypes; ++J)
+    for (int K = J; K < P.ntypes; ++K) {
+      const AngP& A = P.ang[I][lidx(J, K)];
+      if (A.n == 0) continue;
+      const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
+      const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
+      block_pair_factors<true>(S, A, j0, j0 + nJ, cap, false);
+      if (K != J) block_pair_factors<true>(S, A, k0, k0 + nK, cap, false);
+      __syncwarp();
+      tangent_block<NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
+      __syncwarp();
+      for (int f = lane; f < A.n; f += 32) Ui[A.off + f] = -A.norm * S.scratch[A.gidx[f]];
+      __syncwarp();
+    }
+}
+
+template <int NEK, int NZK>
+static void launch_tangent_t(const BatchDev& B, const PotParams& P, const float4* tvec, float* U, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) attr = cudaFuncSetAttribute(tangent_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  const int warps = 4;
+  tangent_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, sizeof(float) * warp_smem_floats(B.cap, NEK, true) * warps, st>>>(
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_code, B.nb_cnt, tvec, U, B.gstride);
+}
+
+// The kernel instance must cover every block's zeta chain: the moment blocks' zeta <= 4 (nz 3)
+// included, which nz (the triplet blocks' largest) does not count.
+int launch_tangent(const BatchDev& B, const PotParams& P, int ne, int nz, const float4* tvec, float* U, cudaStream_t st) {
+  if (B.natoms == 0) return 0;
+  nz = nz < 3 ? 3 : nz;
+  if (ne <= 2 && nz <= 5) launch_tangent_t<2, 5>(B, P, tvec, U, st);
+  else if (ne <= 4 && nz <= 5) launch_tangent_t<4, 5>(B, P, tvec, U, st);
+  else if (ne <= 4 && nz <= 6) launch_tangent_t<4, 6>(B, P, tvec, U, st);
+  else return -1;
+  return 0;
+}
+
 size_t symm_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne, false) * warps; }
 size_t force_smem_bytes(int cap, int ne, int warps, bool kx) { return sizeof(float) * warp_smem_floats(cap, ne, kx) * warps; }
 

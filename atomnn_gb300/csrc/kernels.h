@@ -83,6 +83,15 @@ int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weight
 int train_tiles(int natoms, int ntypes);
 int launch_train(const BatchDev& B, const NetsP& N, int ntypes, const double* eref, int loss, double delta, double* dcdo, double* err,
                  float* partial, int pstride, double* grad, int max_params, cudaStream_t st);
+// the force trainer: residual weights t_k = beta (F_k - F_ref,k)/N^2, the loss terms, the
+// descriptor-space weights u (tangent_kernel) and the parameter gradient of the force term
+// accumulated onto grad
+int train_force_tiles(int natoms, int ntypes);
+void launch_train_force_loss(const BatchDev& B, const double* fref, double beta, float4* tvec, double* fatom, double* fstruc, double* err,
+                             cudaStream_t st);
+int launch_tangent(const BatchDev& B, const PotParams& P, int ne, int nz, const float4* tvec, float* U, cudaStream_t st);
+int launch_train_force(const BatchDev& B, const NetsP& N, int ntypes, const float* U, float* partial, int pstride, double* grad,
+                       int max_params, cudaStream_t st);
 // force gather, orphan fix-up, per-structure energy
 void launch_gather(const BatchDev& B, const NetsP& N, bool add_vacuum, bool want_force, cudaStream_t st);
 

@@ -454,9 +454,9 @@ __global__ void __launch_bounds__(128) train_grad_kernel(const __grid_constant__
   }
 }
 
-// grad[goff[t] + q] = sum over the tiles of species t, in tile order, of partial[tile][q]
+// grad[goff[t] + q] (+)= sum over the tiles of species t, in tile order, of partial[tile][q]
 __global__ void train_reduce_kernel(const __grid_constant__ NetsP N, int ntypes, int tile, const int* __restrict__ tc,
-                                    const float* __restrict__ partial, int pstride, double* __restrict__ grad) {
+                                    const float* __restrict__ partial, int pstride, double* __restrict__ grad, int accumulate) {
   int t = blockIdx.y, first = 0, goff = 0;
   if (t >= ntypes) return;
   for (int ty = 0; ty < t; ++ty) {
@@ -469,7 +469,7 @@ __global__ void train_reduce_kernel(const __grid_constant__ NetsP N, int ntypes,
   if (q >= np) return;
   double s = 0.0;
   for (int k = 0; k < ntiles; ++k) s += (double)partial[(size_t)(first + k) * pstride + q];
-  grad[goff + q] = s;
+  grad[goff + q] = accumulate ? grad[goff + q] + s : s;
 }
 
 constexpr int TRAIN_TILE = 64;
@@ -496,7 +496,251 @@ int launch_train(const BatchDev& B, const NetsP& N, int ntypes, const double* er
   if (smem > 200 * 1024) return -1;
   train_grad_kernel<TRAIN_TILE><<<train_tiles(B.natoms, ntypes), 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride,
                                                                                     B.atom_struc, B.s0, dcdo, partial, pstride);
-  train_reduce_kernel<<<dim3((max_params + 127) / 128, ntypes), 128, 0, st>>>(N, ntypes, TRAIN_TILE, B.type_count, partial, pstride, grad);
+  train_reduce_kernel<<<dim3((max_params + 127) / 128, ntypes), 128, 0, st>>>(N, ntypes, TRAIN_TILE, B.type_count, partial, pstride, grad, 0);
+  return 0;
+}
+
+// ------------------------------------------------------------------------- force training
+// Per atom: fdiff = (F - F_ref)/N (nnptef.cpp:1163-1166), t = beta fdiff / N (dloss/dF),
+// fatom = |fdiff|^2.
+__global__ void train_force_diff_kernel(int a0, int natoms, int s0, const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
+                                        const double* __restrict__ force, const double* __restrict__ fref, double beta,
+                                        float4* __restrict__ tvec, double* __restrict__ fatom) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= natoms) return;
+  const int i = a0 + k;
+  const double norm = 1.0 / meta[atom_struc[i]].natoms;
+  double f2 = 0.0, t[3];
+  for (int x = 0; x < 3; ++x) {
+    const double fd = (force[3 * (size_t)i + x] - fref[3 * (size_t)i + x]) * norm;
+    f2 += fd * fd;
+    t[x] = beta * fd * norm;
+  }
+  tvec[i] = make_float4((float)t[0], (float)t[1], (float)t[2], 0.f);
+  fatom[i] = f2;
+}
+
+// one CTA per structure: fstruc[s] = sum of fatom over its atoms (fixed order)
+__global__ void __launch_bounds__(256) train_force_struc_kernel(int s0, const StrucMeta* __restrict__ meta, const double* __restrict__ fatom,
+                                                                double* __restrict__ fstruc) {
+  __shared__ double red[8];
+  const StrucMeta& S = meta[s0 + blockIdx.x];
+  double v = 0.0;
+  for (int a = threadIdx.x; a < S.natoms; a += blockDim.x) v += fatom[S.atom0 + a];
+  v = warp_sum_d(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    fstruc[blockIdx.x] = t;
+  }
+}
+
+// err[0] += 0.5 beta sum_s fstruc, err[2] = sum_s fstruc (tree order fixed)
+__global__ void train_force_err_kernel(int nstruc, const double* __restrict__ fstruc, double beta, double* __restrict__ err) {
+  __shared__ double r[256];
+  double v = 0.0;
+  for (int s = threadIdx.x; s < nstruc; s += blockDim.x) v += fstruc[s];
+  r[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) r[threadIdx.x] += r[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    err[0] += 0.5 * beta * r[0];
+    err[2] = r[0];
+  }
+}
+
+void launch_train_force_loss(const BatchDev& B, const double* fref, double beta, float4* tvec, double* fatom, double* fstruc, double* err,
+                             cudaStream_t st) {
+  if (B.natoms == 0) return;
+  train_force_diff_kernel<<<(B.natoms + 255) / 256, 256, 0, st>>>(B.a0, B.natoms, B.s0, B.atom_struc, B.meta, B.force, fref, beta, tvec, fatom);
+  train_force_struc_kernel<<<B.nstruc, 256, 0, st>>>(B.s0, B.meta, fatom, fstruc);
+  train_force_err_kernel<<<1, 256, 0, st>>>(B.nstruc, fstruc, beta, err);
+}
+
+// activation derivatives from the activation value a: first and second
+__device__ __forceinline__ void act_d12(int act, float a, float& d1, float& d2) {
+  if (act == ACT_TANH) {
+    d1 = 1.0f - a * a;
+    d2 = -2.0f * a * d1;
+  } else if (act == ACT_SIGMOID) {
+    d1 = a * (1.0f - a);
+    d2 = d1 * (1.0f - 2.0f * a);
+  } else {
+    d1 = 1.0f;
+    d2 = 0.f;
+  }
+}
+
+// Parameter gradient of sum_atoms u . d out/d G for one tile of TILE atoms of one species: the
+// networks' mixed second derivative (D2ODZDI, src/ml/nn.cpp:1789-1890) contracted with u, by a
+// forward tangent inpw .* u through the layers and a reverse pass over the primal and tangent
+// chains.  smem per hidden layer l: A (activation), TA (tangent activation), TZ (tangent
+// pre-activation), DP and DT (adjoints of the pre-activation and of its tangent); X0/TX0 the
+// scaled inputs and their tangents.  The output layer is linear with one node: its tangent
+// adjoint is outw and its primal adjoint zero.  The first-layer weight term keeps inpw
+// (D2ODZDI::grad, nn.cpp:1854-1862, leaves it out).
+template <int TILE>
+__global__ void __launch_bounds__(128) train_force_kernel(const __grid_constant__ NetsP N, int ntypes, const int* __restrict__ tc,
+                                                          const int* __restrict__ perm, const float* __restrict__ G,
+                                                          const float* __restrict__ U, int gstride, float* __restrict__ partial, int pstride) {
+  extern __shared__ float sm[];
+  int t = -1, start = 0, cnt = 0, rem = blockIdx.x;
+  for (int ty = 0; ty < ntypes; ++ty) {
+    const int c = tc[ty];
+    const int nt = (c + TILE - 1) / TILE;
+    if (rem < nt) { t = ty; start = tc[NT_MAX + 1 + ty] + rem * TILE; cnt = min(TILE, c - rem * TILE); break; }
+    rem -= nt;
+  }
+  if (t < 0) return;
+  const NetP& net = N.net[t];
+  const int L = net.nlayer, K0 = net.nin, H = L - 1;  // H hidden layers
+  float* X0 = sm;
+  float* TX0 = X0 + K0 * TILE;
+  float *A[NLAYER_MAX], *TA[NLAYER_MAX], *TZ[NLAYER_MAX], *DP[NLAYER_MAX], *DT[NLAYER_MAX];
+  float* p = TX0 + K0 * TILE;
+  for (int l = 0; l < H; ++l) {
+    const int sz = net.nodes[l] * TILE;
+    A[l] = p; TA[l] = p + sz; TZ[l] = p + 2 * sz; DP[l] = p + 3 * sz; DT[l] = p + 4 * sz;
+    p += 5 * sz;
+  }
+  for (int w = threadIdx.x; w < K0 * TILE; w += blockDim.x) {
+    const int k = w / TILE, a = w % TILE;
+    const bool on = a < cnt;
+    const size_t row = on ? (size_t)perm[start + a] * gstride : 0;
+    X0[w] = on ? net.inpw[k] * (G[row + k] + net.inpb[k]) : 0.f;
+    TX0[w] = on ? net.inpw[k] * U[row + k] : 0.f;
+  }
+  __syncthreads();
+  // forward: primal and tangent
+  const float* in = X0;
+  const float* tin = TX0;
+  int Kl = K0;
+  for (int l = 0; l < H; ++l) {
+    tile_gemm<TILE>(in, Kl, net.wt[l], net.nodes[l], net.nodes[l], A[l], net.b[l]);
+    tile_gemm<TILE>(tin, Kl, net.wt[l], net.nodes[l], net.nodes[l], TZ[l], nullptr);
+    __syncthreads();
+    for (int w = threadIdx.x; w < net.nodes[l] * TILE; w += blockDim.x) {
+      float a, d;
+      act_fd(net.act, A[l][w], a, d);
+      A[l][w] = a;
+      TA[l][w] = d * TZ[l][w];
+    }
+    __syncthreads();
+    in = A[l];
+    tin = TA[l];
+    Kl = net.nodes[l];
+  }
+  // top hidden layer: adjoint of its tangent activation = outw * w_out; of its activation 0
+  {
+    const int l = H - 1;
+    const float* wout = net.w[L - 1];
+    for (int w = threadIdx.x; w < net.nodes[l] * TILE; w += blockDim.x) {
+      const int c = w / TILE;
+      float d1, d2;
+      act_d12(net.act, A[l][w], d1, d2);
+      const float g = net.outw * wout[c];
+      DT[l][w] = d1 * g;
+      DP[l][w] = d2 * TZ[l][w] * g;
+    }
+    __syncthreads();
+  }
+  for (int l = H - 1; l > 0; --l) {
+    tile_gemm<TILE>(DT[l], net.nodes[l], net.w[l], net.nodes[l - 1], net.nodes[l - 1], DT[l - 1], nullptr);
+    tile_gemm<TILE>(DP[l], net.nodes[l], net.w[l], net.nodes[l - 1], net.nodes[l - 1], DP[l - 1], nullptr);
+    __syncthreads();
+    for (int w = threadIdx.x; w < net.nodes[l - 1] * TILE; w += blockDim.x) {
+      float d1, d2;
+      act_d12(net.act, A[l - 1][w], d1, d2);
+      const float st = DT[l - 1][w];
+      DT[l - 1][w] = d1 * st;
+      DP[l - 1][w] = d1 * DP[l - 1][w] + d2 * TZ[l - 1][w] * st;
+    }
+    __syncthreads();
+  }
+  // the tile's gradient: bias(l, n) = sum_a DP[l][n][a]; weight(l, n, m) = sum_a DT[l][n][a] TX_l[m][a] +
+  // DP[l][n][a] X_l[m][a]; the output layer: bias 0, weight(m) = outw sum_a TA[H-1][m][a]
+  float* out = partial + (size_t)blockIdx.x * pstride;
+  int nb = 0;
+  for (int l = 0; l < L; ++l) nb += net.nodes[l];
+  const int np = net_params(net);
+  for (int q = threadIdx.x; q < np; q += blockDim.x) {
+    int l = 0, r = q, n, m = -1;
+    if (r < nb) {
+      while (r >= net.nodes[l]) { r -= net.nodes[l]; ++l; }
+      n = r;
+    } else {
+      r -= nb;
+      while (r >= net.nodes[l] * (l == 0 ? K0 : net.nodes[l - 1])) { r -= net.nodes[l] * (l == 0 ? K0 : net.nodes[l - 1]); ++l; }
+      m = r / net.nodes[l];
+      n = r % net.nodes[l];
+    }
+    float s = 0.f;
+    if (l == L - 1) {
+      if (m >= 0) {
+        const float4* x4 = reinterpret_cast<const float4*>(TA[H - 1] + m * TILE);
+#pragma unroll 4
+        for (int v = 0; v < TILE / 4; ++v) {
+          const float4 x = x4[v];
+          s += (x.x + x.y) + (x.z + x.w);
+        }
+        s *= net.outw;
+      }
+    } else if (m < 0) {
+      const float4* d4 = reinterpret_cast<const float4*>(DP[l] + n * TILE);
+#pragma unroll 4
+      for (int v = 0; v < TILE / 4; ++v) {
+        const float4 x = d4[v];
+        s += (x.x + x.y) + (x.z + x.w);
+      }
+    } else {
+      const float4* dp4 = reinterpret_cast<const float4*>(DP[l] + n * TILE);
+      const float4* dt4 = reinterpret_cast<const float4*>(DT[l] + n * TILE);
+      const float4* x4 = reinterpret_cast<const float4*>((l == 0 ? X0 : A[l - 1]) + m * TILE);
+      const float4* tx4 = reinterpret_cast<const float4*>((l == 0 ? TX0 : TA[l - 1]) + m * TILE);
+#pragma unroll 4
+      for (int v = 0; v < TILE / 4; ++v) {
+        const float4 a = dp4[v], b = x4[v], c = dt4[v], d = tx4[v];
+        s = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, s))));
+        s = fmaf(c.x, d.x, fmaf(c.y, d.y, fmaf(c.z, d.z, fmaf(c.w, d.w, s))));
+      }
+    }
+    out[q] = s;
+  }
+}
+
+constexpr int TRAIN_FORCE_TILE = 32;
+
+static size_t train_force_smem_bytes(const NetsP& N, int ntypes) {
+  size_t floats = 0;
+  for (int t = 0; t < ntypes; ++t) {
+    const NetP& n = N.net[t];
+    size_t f = (size_t)2 * n.nin * TRAIN_FORCE_TILE;
+    for (int l = 0; l < n.nlayer - 1; ++l) f += (size_t)5 * n.nodes[l] * TRAIN_FORCE_TILE;
+    floats = floats > f ? floats : f;
+  }
+  return floats * sizeof(float);
+}
+
+int train_force_tiles(int natoms, int ntypes) { return (natoms + TRAIN_FORCE_TILE - 1) / TRAIN_FORCE_TILE + ntypes; }
+
+int launch_train_force(const BatchDev& B, const NetsP& N, int ntypes, const float* U, float* partial, int pstride, double* grad,
+                       int max_params, cudaStream_t st) {
+  const size_t smem = train_force_smem_bytes(N, ntypes);
+  if (smem > 200 * 1024) return -1;
+  for (int t = 0; t < ntypes; ++t)
+    if (N.net[t].nlayer < 2) return -1;
+  static bool attr = false;
+  if (!attr)
+    attr = cudaFuncSetAttribute(train_force_kernel<TRAIN_FORCE_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
+  train_force_kernel<TRAIN_FORCE_TILE><<<train_force_tiles(B.natoms, ntypes), 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, U,
+                                                                                              B.gstride, partial, pstride);
+  train_reduce_kernel<<<dim3((max_params + 127) / 128, ntypes), 128, 0, st>>>(N, ntypes, TRAIN_FORCE_TILE, B.type_count, partial, pstride,
+                                                                             grad, 1);
   return 0;
 }
 

@@ -587,7 +587,8 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
                     &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
-                    &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in};
+                    &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in, &c->tr_fref, &c->tr_t,
+                    &c->tr_fatom, &c->tr_fstruc, &c->tr_u};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);
@@ -976,6 +977,63 @@ extern "C" int nnpgpu_train_grad(nnpgpu_ctx* c, int nstruc, const int* natoms, c
   cudaMemcpyAsync(grad, c->tr_grad.p, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
   const cudaError_t err = cudaStreamSynchronize(st);
   if (err != cudaSuccess) return cuda_fail(c, err, "train");
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_train_force_grad(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species,
+                                       const double* cell, const double* energy_ref, const double* force_ref, double beta, int loss,
+                                       double delta, double* error, double* grad) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  if (nstruc <= 0 || !energy_ref || !force_ref || !error || !grad) return set_error(c, NNPGPU_ERR_INVALID, "train_force: invalid arguments");
+  if (loss < 0 || loss > 3) return set_error(c, NNPGPU_ERR_INVALID, "train_force: loss must be 0 (MSE), 1 (MAE), 2 (HUBER) or 3 (ASINH)");
+  if ((loss >= 2) && !(delta > 0)) return set_error(c, NNPGPU_ERR_INVALID, "train_force: HUBER and ASINH need delta > 0");
+  if (!(beta >= 0) || !std::isfinite(beta)) return set_error(c, NNPGPU_ERR_INVALID, "train_force: beta must be finite and >= 0");
+  size_t N = 0;
+  for (int s = 0; s < nstruc; ++s) {
+    if (!natoms || natoms[s] <= 0) return set_error(c, NNPGPU_ERR_INVALID, "train_force: every structure needs atoms");
+    N += (size_t)natoms[s];
+  }
+  std::vector<double> e(nstruc), F(3 * N);
+  int rc = compute_impl(c, nstruc, natoms, posn, species, cell, NNPGPU_ENERGY | NNPGPU_FORCE | NNPGPU_BATCHED | NNPGPU_NO_VACUUM, e.data(),
+                        F.data(), nullptr, false, nullptr);
+  if (rc != NNPGPU_OK) return rc;
+  cudaStream_t st = c->stream;
+  int total = 0, maxp = 0;
+  for (int t = 0; t < c->pot.ntypes; ++t) {
+    total += net_param_count(c, t);
+    maxp = std::max(maxp, net_param_count(c, t));
+  }
+  const int pstride = (maxp + 3) / 4 * 4;
+  const Uploaded& U = c->meta_cache.U;
+  const int tiles = std::max(train_tiles(U.natoms, c->pot.ntypes), train_force_tiles(U.natoms, c->pot.ntypes));
+  if (!ensure(c, c->tr_eref, sizeof(double) * nstruc) || !ensure(c, c->tr_dcdo, sizeof(double) * nstruc) ||
+      !ensure(c, c->tr_err, sizeof(double) * 3) || !ensure(c, c->tr_part, sizeof(float) * (size_t)tiles * pstride) ||
+      !ensure(c, c->tr_grad, sizeof(double) * total) || !ensure(c, c->tr_fref, sizeof(double) * 3 * N) ||
+      !ensure(c, c->tr_t, sizeof(float4) * N) || !ensure(c, c->tr_fatom, sizeof(double) * N) ||
+      !ensure(c, c->tr_fstruc, sizeof(double) * nstruc) || !ensure(c, c->tr_u, sizeof(float) * N * c->gstride))
+    return set_error(c, NNPGPU_ERR_OOM, "train_force: device allocation failed or HBM budget exceeded");
+  BatchDev B = batch_view(c, U, (const double*)c->posn.p, (const int*)c->type.p, (double*)c->energy.p, (double*)c->force.p);
+  cudaMemcpyAsync(c->tr_eref.p, energy_ref, sizeof(double) * nstruc, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->tr_fref.p, force_ref, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st);
+  // energy term: loss, dc/dout and the gradient written into tr_grad
+  if (launch_train(B, c->nets, c->pot.ntypes, (const double*)c->tr_eref.p, loss, delta, (double*)c->tr_dcdo.p, (double*)c->tr_err.p,
+                   (float*)c->tr_part.p, pstride, (double*)c->tr_grad.p, maxp, st) != 0)
+    return set_error(c, NNPGPU_ERR_UNSUPPORTED, "train_force: networks too wide for the gradient kernel's shared memory");
+  // force term: residual weights, loss, descriptor-space weights, then the gradient added
+  launch_train_force_loss(B, (const double*)c->tr_fref.p, beta, (float4*)c->tr_t.p, (double*)c->tr_fatom.p, (double*)c->tr_fstruc.p,
+                          (double*)c->tr_err.p, st);
+  if (launch_tangent(B, c->P, c->ne, c->nz, (const float4*)c->tr_t.p, (float*)c->tr_u.p, st) != 0)
+    return set_error(c, NNPGPU_ERR_UNSUPPORTED, "train_force: no tangent kernel instance");
+  if (launch_train_force(B, c->nets, c->pot.ntypes, (const float*)c->tr_u.p, (float*)c->tr_part.p, pstride, (double*)c->tr_grad.p, maxp,
+                         st) != 0)
+    return set_error(c, NNPGPU_ERR_UNSUPPORTED, "train_force: networks too wide for the force-gradient kernel's shared memory");
+  const cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) return cuda_fail(c, le, "train_force launch");
+  cudaMemcpyAsync(error, c->tr_err.p, sizeof(double) * 3, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(grad, c->tr_grad.p, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+  const cudaError_t err = cudaStreamSynchronize(st);
+  if (err != cudaSuccess) return cuda_fail(c, err, "train_force");
   return NNPGPU_OK;
 }
 

@@ -19,7 +19,8 @@ EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntype
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
            "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
-           "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad", "nnpgpu_energy_symm"]
+           "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad", "nnpgpu_energy_symm",
+           "nnpgpu_train_force_grad"]
 
 _lib = None
 
@@ -73,6 +74,7 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_nparams.argtypes = [vp, ip]
     L.nnpgpu_train_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, ip, dp, vp, vp]
     L.nnpgpu_energy_symm.argtypes = [vp, ip, vp, vp, vp, ip, ip, vp]
+    L.nnpgpu_train_force_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp, dp, ip, dp, vp, vp]
     L.nnpgpu_md_destroy.argtypes = [vp]
     L.nnpgpu_md_destroy.restype = None
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
@@ -207,6 +209,21 @@ class Engine:
         self._check(self.lib.nnpgpu_train_grad(self._ctx, len(structures), _p(natoms), _p(posn), _p(species), _p(cell), _p(eref),
                                                self.LOSS[loss], float(delta), _p(err), _p(grad)))
         return err[0], err[1], grad
+
+    def train_force_grad(self, structures, energy_ref, force_ref, beta, loss="MSE", delta=1.0):
+        """(loss, sum of dE^2, sum of |dF/N|^2, gradient) of one batch with forces
+        (nnpgpu_train_force_grad); force_ref: one (N,3) array per structure."""
+        natoms = np.array([s.posn.shape[0] for s in structures], dtype=np.int32)
+        posn = np.ascontiguousarray(np.concatenate([np.asarray(s.posn, dtype=np.float64) for s in structures]))
+        species = np.ascontiguousarray(np.concatenate([np.asarray(s.species, dtype=np.int32) for s in structures]))
+        cell = np.ascontiguousarray(np.concatenate([_cell_colmajor(s.cell) for s in structures]))
+        eref = np.ascontiguousarray(energy_ref, dtype=np.float64)
+        fref = np.ascontiguousarray(np.concatenate([np.asarray(f, dtype=np.float64) for f in force_ref]))
+        err = np.zeros(3)
+        grad = np.zeros(sum(self.nparams(t) for t in range(self.ntypes)))
+        self._check(self.lib.nnpgpu_train_force_grad(self._ctx, len(structures), _p(natoms), _p(posn), _p(species), _p(cell), _p(eref),
+                                                     _p(fref), float(beta), self.LOSS[loss], float(delta), _p(err), _p(grad)))
+        return err[0], err[1], err[2], grad
 
     def energy_symm(self, natoms, species, symm, flags=0):
         """Energies of structures from stored descriptors (nnpgpu_energy_symm): natoms per

@@ -141,6 +141,16 @@ int nnpgpu_energy_symm(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const int
  *   layer's weights with the input index outer and the node index inner).
  * Descriptors are computed from the positions on each call (FP32, FP32 networks). */
 int nnpgpu_nparams(const nnpgpu_ctx* ctx, int type);
+/* ---- training with forces: the force trainer's loss (NNPTEF::error, src/nnp/nnptef.cpp:1043-1135)
+ *   sum_s loss(dE_s) + sum over atoms 0.5 beta |(F - F_ref)/N_s|^2,
+ * F the forces of NNP::force (minimum-image rule), E without vacuum energies, loss and delta as
+ * for nnpgpu_train_grad; force_ref[sum(natoms)*3].  grad is the exact gradient of that loss (the
+ * reference's nnptef.cpp keeps only each atom's own terms and calls BasisR::rho, which this
+ * snapshot does not define); error[0] = the loss, error[1] = sum of dE^2, error[2] = sum over
+ * atoms of |(F - F_ref)/N_s|^2.  FP32 descriptors, networks and second derivatives, FP64 sums. */
+int nnpgpu_train_force_grad(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* posn, const int* species,
+                            const double* cell, const double* energy_ref, const double* force_ref, double beta, int loss,
+                            double delta, double* error, double* grad);
 int nnpgpu_train_grad(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double* posn, const int* species,
                       const double* cell, const double* energy_ref, int loss, double delta, double* error, double* grad);
 

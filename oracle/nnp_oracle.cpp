@@ -181,6 +181,16 @@ struct BasisR : Basis {
     }
     return amp * norm;
   }
+  // d G_m / d r for every function m: the term BasisR::force contracts with dE/dG (force
+  // returns -sum_m dEdG_m dG_m/dr); evaluated through force with a unit dE/dG per function.
+  void dval(double dr, double* out) const {
+    std::vector<double> unit(size, 0.0);
+    for (int m = 0; m < size; ++m) {
+      unit[m] = 1.0;
+      out[m] = -force(dr, unit.data());
+      unit[m] = 0.0;
+    }
+  }
 };
 
 struct BasisA : Basis {
@@ -248,6 +258,43 @@ struct BasisA : Basis {
     }
     phi_o *= norm; eta_o[0] *= norm; eta_o[1] *= norm; eta_o[2] *= norm;
   }
+  // Per function m the three values BasisA::force sums over functions, for a unit dE/dG_m:
+  // phif[m] = -dG_m/dcos, e0[m] = -dG_m/dr_ij, e1[m] = -dG_m/dr_ik (the expressions of force,
+  // basis_angular.cpp:456-640, and of BasisA::forcep, basis_angular.cpp:642-761, with the sign of force).
+  void dfunc(double cs, const double d[3], double* phif, double* e0, double* e1) const {
+    const double c[2] = {cut_func(d[0]), cut_func(d[1])};
+    const double g[2] = {cut_grad(d[0]), cut_grad(d[1])};
+    const double cprod = c[0] * c[1];
+    const double rijp = powint(d[0], alpha), rikp = powint(d[1], alpha);
+    const double dij = alpha * rijp / d[0] * c[0];
+    const double dik = alpha * rikp / d[1] * c[1];
+    for (int i = 0; i < size; ++i) {
+      double fr = 0, dj = 0, dk = 0;
+      switch (phi) {
+        case PA_GAUSS: fr = std::exp(-ietap[i] * (rijp + rikp)); dj = ietap[i]; dk = ietap[i]; break;
+        case PA_IPOWP: {
+          const double denij = 1.0 / (1.0 + ietap[i] * rijp), denik = 1.0 / (1.0 + ietap[i] * rikp);
+          fr = denij * denik; dj = ietap[i] * denij; dk = ietap[i] * denik;
+        } break;
+        case PA_IPOWS: { const double den = 1.0 / (1.0 + ietap[i] * (rijp + rikp)); fr = den; dj = ietap[i] * den; dk = dj; } break;
+        case PA_SECHP: {
+          const double sij = sech(ietap[i] * rijp), sik = sech(ietap[i] * rikp);
+          fr = sij * sik; dj = ietap[i] * std::sqrt(1.0 - sij * sij); dk = ietap[i] * std::sqrt(1.0 - sik * sik);
+        } break;
+        case PA_SECHS: {
+          const double sv = sech(ietap[i] * (rijp + rikp));
+          fr = sv; dj = ietap[i] * std::sqrt(1.0 - sv * sv); dk = dj;
+        } break;
+        default: throw std::invalid_argument("BasisA::force: invalid symmetry function");
+      }
+      const double cw = std::fabs(0.5 * (1.0 + lambda[i] * cs));
+      const double gangle = std::pow(cw, zeta[i] - 1.0) * fr;
+      const double fangle = cw * gangle;
+      phif[i] = -0.5 * zeta[i] * lambda[i] * cprod * gangle * norm;
+      e0[i] = -fangle * (-dij * dj + g[0]) * c[1] * norm;
+      e1[i] = -fangle * (-dik * dk + g[1]) * c[0] * norm;
+    }
+  }
 };
 
 // ---------------------------------------------------------------- network
@@ -309,6 +356,80 @@ struct ANN {
       }
     }
     return out;
+  }
+  // second derivative of the activation from its value a (AFFPBP's d2adz2 for tanh, sigmoid, linear)
+  static double act2(int neuron, double a) {
+    switch (neuron) {
+      case N_TANH: return -2.0 * a * (1.0 - a * a);
+      case N_SIGMOID: return a * (1.0 - a) * (1.0 - 2.0 * a);
+      default: return 0.0;
+    }
+  }
+  // grad += d/d parameter of (u . d out / d inp) at inp: the parameter gradient of the force term
+  // of the loss (the mixed second derivative D2ODZDI of src/ml/nn.cpp:1789-1890, contracted with
+  // u).  Forward-mode tangent inpw .* u through the layers, then reverse mode over both the
+  // primal and the tangent chain.  Exact: the inpw factor of the first-layer weight term is kept
+  // (D2ODZDI::grad, nn.cpp:1854-1862, leaves it out).
+  void force_param_grad(const double* inp, const double* u, double* grad) const {
+    const int L = nlayer();
+    std::vector<double> ins(nin), tin(nin);
+    for (int k = 0; k < nin; ++k) { ins[k] = inpw[k] * (inp[k] + inpb[k]); tin[k] = inpw[k] * u[k]; }
+    std::vector<std::vector<double>> a(L), ta(L), tz(L), d1(L);
+    for (int l = 0; l < L; ++l) {
+      const int R = nodes[l], C = cols(l);
+      const std::vector<double>& x = (l == 0) ? ins : a[l - 1];
+      const std::vector<double>& tx = (l == 0) ? tin : ta[l - 1];
+      a[l].resize(R); ta[l].resize(R); tz[l].resize(R); d1[l].resize(R);
+      const int nl = (l == L - 1) ? N_LINEAR : neuron;
+      for (int r = 0; r < R; ++r) {
+        double z = b[l][r], t = 0;
+        for (int c = 0; c < C; ++c) { z += w[l][(size_t)r * C + c] * x[c]; t += w[l][(size_t)r * C + c] * tx[c]; }
+        act(nl, z, a[l][r], d1[l][r]);
+        tz[l][r] = t;
+        ta[l][r] = d1[l][r] * t;
+      }
+    }
+    // h = outw . tangent of the last layer; adjoints dt (of the tangent pre-activations) and dp
+    // (of the primal pre-activations)
+    std::vector<std::vector<double>> dt(L), dp(L);
+    dt[L - 1].assign(nodes[L - 1], 0.0);
+    dp[L - 1].assign(nodes[L - 1], 0.0);
+    for (int r = 0; r < nodes[L - 1]; ++r) dt[L - 1][r] = outw[r] * d1[L - 1][r];  // linear: d1 = 1, act2 = 0
+    for (int l = L - 1; l > 0; --l) {
+      const int R = nodes[l], C = cols(l);
+      dt[l - 1].assign(C, 0.0);
+      dp[l - 1].assign(C, 0.0);
+      for (int c = 0; c < C; ++c) {
+        double st = 0, sp = 0;
+        for (int r = 0; r < R; ++r) { st += w[l][(size_t)r * C + c] * dt[l][r]; sp += w[l][(size_t)r * C + c] * dp[l][r]; }
+        dt[l - 1][c] = d1[l - 1][c] * st;
+        dp[l - 1][c] = d1[l - 1][c] * sp + act2(neuron, a[l - 1][c]) * tz[l - 1][c] * st;
+      }
+    }
+    int count = 0;
+    for (int l = 0; l < L; ++l)
+      for (int n = 0; n < nodes[l]; ++n) grad[count++] += dp[l][n];
+    for (int l = 0; l < L; ++l) {
+      const int R = nodes[l], C = cols(l);
+      for (int m = 0; m < C; ++m) {
+        const double x = (l > 0) ? a[l - 1][m] : ins[m];
+        const double tx = (l > 0) ? ta[l - 1][m] : tin[m];
+        for (int n = 0; n < R; ++n) grad[count++] += dp[l][n] * x + dt[l][n] * tx;
+      }
+    }
+  }
+  // parameters in the reference's order (ANN::size, Cost::grad)
+  void get_params(double* p) const {
+    int count = 0;
+    for (int l = 0; l < nlayer(); ++l) for (int n = 0; n < nodes[l]; ++n) p[count++] = b[l][n];
+    for (int l = 0; l < nlayer(); ++l)
+      for (int m = 0; m < cols(l); ++m) for (int n = 0; n < nodes[l]; ++n) p[count++] = w[l][(size_t)n * cols(l) + m];
+  }
+  void set_params(const double* p) {
+    int count = 0;
+    for (int l = 0; l < nlayer(); ++l) for (int n = 0; n < nodes[l]; ++n) b[l][n] = p[count++];
+    for (int l = 0; l < nlayer(); ++l)
+      for (int m = 0; m < cols(l); ++m) for (int n = 0; n < nodes[l]; ++n) w[l][(size_t)n * cols(l) + m] = p[count++];
   }
   // ANN::size (src/ml/nn.cpp:899-905): biases of every layer, then weights
   int size() const {
@@ -857,6 +978,64 @@ static double force(NNP& nnp, int natoms, const int* type, const std::vector<std
   return energy;
 }
 
+// u_i[f] = sum_k t_k . C_ifk, where C_ifk is the force on atom k per unit dE/dG_if in NNP::force
+// (nnp.cpp:416-482, minimum-image rule included): the descriptor-space weights of the force
+// term of the loss, t_k = dloss/dF_k.
+static void force_tangent(NNP& nnp, int natoms, const int* type, const std::vector<std::vector<Nb>>& nl, const std::vector<V3>& t,
+                          std::vector<std::vector<double>>& u) {
+  u.assign(natoms, {});
+  for (int i = 0; i < natoms; ++i) {
+    const NNH& h = nnp.nnh[type[i]];
+    u[i].assign(h.nInput, 0.0);
+    const std::vector<Nb>& L = nl[i];
+    std::vector<double> dv(64), pf(64), e0(64), e1(64);
+    for (size_t j = 0; j < L.size(); ++j) {
+      const int JJ = type[L[j].index];
+      const int jj = L[j].index;
+      const bool jmin = L[j].min;
+      const V3& rIJ = L[j].r;
+      const double dIJ = L[j].dr, dIJi = 1.0 / dIJ;
+      {
+        const BasisR& bR = h.basisR[JJ];
+        dv.resize(std::max(bR.size, 1));
+        bR.dval(dIJ, dv.data());
+        // amp_m = -dG_m/dr / r: F_i += amp rIJ, F_j -= amp rIJ (minimum image only)
+        const double proj = dot(t[i], rIJ) - (jmin ? dot(t[jj], rIJ) : 0.0);
+        for (int m = 0; m < bR.size; ++m) u[i][h.offsetR[JJ] + m] += -dv[m] * dIJi * proj;
+      }
+      for (size_t k = j + 1; k < L.size(); ++k) {
+        const int KK = type[L[k].index];
+        const int kk = L[k].index;
+        const bool kmin = L[k].min;
+        const V3& rIK = L[k].r;
+        const double dIK = L[k].dr, dIKi = 1.0 / dIK;
+        const V3 rJK{rIK[0] - rIJ[0], rIK[1] - rIJ[1], rIK[2] - rIJ[2]};
+        const double dJK = nrm(rJK);
+        const int lk = NNH::lidx(JJ, KK);
+        const BasisA& bA = h.basisA[lk];
+        const int off = h.nInputR + h.offsetA[lk];
+        const double cosIJK = dot(rIJ, rIK) * dIJi * dIKi;
+        const double d[3] = {dIJ, dIK, dJK};
+        const size_t n = std::max(bA.size, 1);
+        pf.resize(n); e0.resize(n); e1.resize(n);
+        bA.dfunc(cosIJK, d, pf.data(), e0.data(), e1.data());
+        const double ti_j = dot(t[i], rIJ) * dIJi, ti_k = dot(t[i], rIK) * dIKi;
+        const double tj_j = jmin ? dot(t[jj], rIJ) * dIJi : 0.0, tj_k = jmin ? dot(t[jj], rIK) * dIKi : 0.0;
+        const double tk_j = kmin ? dot(t[kk], rIJ) * dIJi : 0.0, tk_k = kmin ? dot(t[kk], rIK) * dIKi : 0.0;
+        for (int m = 0; m < bA.size; ++m) {
+          const double phi = pf[m];
+          // centre: (phi (1/dIK - cos/dIJ) + eta0) rIJ/dIJ + (phi (1/dIJ - cos/dIK) + eta1) rIK/dIK
+          double v = (phi * (dIKi - cosIJK * dIJi) + e0[m]) * ti_j + (phi * (dIJi - cosIJK * dIKi) + e1[m]) * ti_k;
+          // j: -[(-phi cos/dIJ + eta0) rIJ/dIJ + phi/dIJ rIK/dIK]; k likewise (eta2 = 0)
+          v -= (-phi * cosIJK * dIJi + e0[m]) * tj_j + phi * dIJi * tj_k;
+          v -= (-phi * cosIJK * dIKi + e1[m]) * tk_k + phi * dIKi * tk_j;
+          u[i][off + m] += v;
+        }
+      }
+    }
+  }
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------- C interface
@@ -1011,6 +1190,88 @@ extern "C" int oracle_train_grad(void* nnpv, int nstruc, const int* natoms, cons
         nnp.nnh[type[a]].nn.param_grad(symm + a * stride, dcdo, grad + goff[type[a]]);
       }
       a0 += natoms[s];
+    }
+    return 0;
+  } catch (...) {
+    return -2;
+  }
+}
+
+extern "C" void oracle_nnp_get_params(const void* nnpv, int type, double* p) { ((const NNP*)nnpv)->nnh[type].nn.get_params(p); }
+extern "C" void oracle_nnp_set_params(void* nnpv, int type, const double* p) { ((NNP*)nnpv)->nnh[type].nn.set_params(p); }
+
+// The force trainer's batch error and gradient: the loss of NNPTEF::error (src/nnp/nnptef.cpp:1043-1135)
+//   sum_s loss(dE_s) + sum_atoms 0.5 beta |(F_nnp - F_ref) / N_s|^2,
+// dE_s = (E_s - E_ref,s)/N_s with E_s the sum of network outputs (no vacuum energies) and F the
+// forces of NNP::force (minimum-image rule), loss as in oracle_train_grad.  grad is the exact
+// gradient of that loss: the energy term as in the energy trainer, the force term through
+// u_i = sum_k t_k . dF_k/d(dE/dG_i) with t_k = beta (F_k - F_ref,k)/N_s^2 and the mixed second
+// derivative of each atom's network (ANN::force_param_grad).  error[0] = the loss, error[1] =
+// sum of dE^2, error[2] = sum over atoms of |(F_nnp - F_ref)/N_s|^2.
+// posn/fref: concatenated N x 3; cells: nstruc x 9 column-major.
+extern "C" int oracle_train_force_grad(void* nnpv, int nstruc, const int* natoms, const double* posn, const int* type, const double* cells,
+                                       const double* eref, const double* fref, double beta, int loss, double delta, double* error,
+                                       double* grad) {
+  try {
+    NNP& nnp = *(NNP*)nnpv;
+    std::vector<size_t> goff(nnp.ntypes + 1, 0);
+    for (int t = 0; t < nnp.ntypes; ++t) goff[t + 1] = goff[t] + nnp.nnh[t].nn.size();
+    for (size_t k = 0; k < goff[nnp.ntypes]; ++k) grad[k] = 0.0;
+    error[0] = error[1] = error[2] = 0.0;
+    size_t a0 = 0;
+    for (int s = 0; s < nstruc; ++s) {
+      const int n = natoms[s];
+      const int* ty = type + a0;
+      for (int i = 0; i < n; ++i)
+        if (ty[i] < 0 || ty[i] >= nnp.ntypes) return -3;
+      Cell cell;
+      cell.init(cells + 9 * (size_t)s);
+      std::vector<V3> p(n);
+      for (int i = 0; i < n; ++i) p[i] = V3{posn[3 * (a0 + i)], posn[3 * (a0 + i) + 1], posn[3 * (a0 + i) + 2]};
+      std::vector<std::vector<Nb>> nl;
+      build_neighbors(cell, n, p.data(), nnp.rc, nl);
+      std::vector<std::vector<double>> G;
+      orc::symm(nnp, n, ty, nl, G);
+      std::vector<V3> F;
+      const double energy = orc::force(nnp, n, ty, nl, G, F);
+      const double norm = 1.0 / n;
+      const double dE = (energy - eref[s]) * norm;
+      double dcdo = norm;
+      switch (loss) {
+        case 0: error[0] += 0.5 * dE * dE; dcdo *= dE; break;
+        case 1: error[0] += std::fabs(dE); dcdo *= (dE > 0) ? 1.0 : ((dE < 0) ? -1.0 : 0.0); break;
+        case 2: {
+          const double arg = dE / delta, sq = std::sqrt(1.0 + arg * arg);
+          error[0] += delta * delta * (sq - 1.0);
+          dcdo *= dE / sq;
+        } break;
+        case 3: {
+          const double arg = dE / delta, sq = std::sqrt(1.0 + arg * arg), lg = std::log(arg + sq);
+          error[0] += delta * delta * (1.0 - sq + arg * lg);
+          dcdo *= lg * delta;
+        } break;
+        default: return -1;
+      }
+      error[1] += dE * dE;
+      std::vector<V3> t(n);
+      for (int i = 0; i < n; ++i) {
+        double f2 = 0;
+        for (int x = 0; x < 3; ++x) {
+          const double fd = (F[i][x] - fref[3 * (a0 + i) + x]) * norm;
+          f2 += fd * fd;
+          t[i][x] = beta * fd * norm;
+        }
+        error[0] += 0.5 * beta * f2;
+        error[2] += f2;
+      }
+      std::vector<std::vector<double>> u;
+      force_tangent(nnp, n, ty, nl, t, u);
+      for (int i = 0; i < n; ++i) {
+        const ANN& nn = nnp.nnh[ty[i]].nn;
+        nn.param_grad(G[i].data(), dcdo, grad + goff[ty[i]]);
+        nn.force_param_grad(G[i].data(), u[i].data(), grad + goff[ty[i]]);
+      }
+      a0 += n;
     }
     return 0;
   } catch (...) {

@@ -63,6 +63,12 @@ double oracle_network(void* nnp, int type, const double* symm, double* dedg);
 int oracle_nnp_nparams(const void* nnp, int type);
 int oracle_train_grad(void* nnp, int nstruc, const int* natoms, const double* symm, int stride, const int* type,
                       const double* eref, int loss, double delta, double* error, double* grad);
+/* network parameters in the reference's order, and the force trainer's batch error and exact
+ * gradient (loss of src/nnp/nnptef.cpp:1043-1135; see nnp_oracle.cpp) */
+void oracle_nnp_get_params(const void* nnp, int type, double* p);
+void oracle_nnp_set_params(void* nnp, int type, const double* p);
+int oracle_train_force_grad(void* nnp, int nstruc, const int* natoms, const double* posn, const int* type, const double* cells,
+                            const double* eref, const double* fref, double beta, int loss, double delta, double* error, double* grad);
 
 #ifdef __cplusplus
 }

@@ -43,6 +43,11 @@ def lib():
         L.oracle_network.restype = dp
         L.oracle_nnp_nparams.argtypes = [vp, ip]
         L.oracle_train_grad.argtypes = [vp, ip, vp, vp, ip, vp, vp, ip, dp, vp, vp]
+        L.oracle_nnp_get_params.argtypes = [vp, ip, vp]
+        L.oracle_nnp_get_params.restype = None
+        L.oracle_nnp_set_params.argtypes = [vp, ip, vp]
+        L.oracle_nnp_set_params.restype = None
+        L.oracle_train_force_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp, dp, ip, dp, vp, vp]
         _lib = L
     return _lib
 
@@ -113,6 +118,34 @@ class OracleNNP:
         if rc != 0:
             raise RuntimeError("oracle_train_grad failed (%d)" % rc)
         return err[0], err[1], grad
+
+    def params(self, t):
+        """Network parameters of type t in the reference's order (biases, then weights input-outer)."""
+        p = np.zeros(lib().oracle_nnp_nparams(self._h, t))
+        lib().oracle_nnp_get_params(self._h, t, _ptr(p))
+        return p
+
+    def set_params(self, t, p):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        assert p.size == lib().oracle_nnp_nparams(self._h, t)
+        lib().oracle_nnp_set_params(self._h, t, _ptr(p))
+
+    def train_force_grad(self, structures, energy_ref, force_ref, beta, loss=0, delta=1.0):
+        """The force trainer's batch error and exact gradient (loss of NNPTEF::error,
+        src/nnp/nnptef.cpp:1043-1135): (loss, sum of dE^2, sum of |dF/N|^2, gradient)."""
+        natoms = np.asarray([s.posn.shape[0] for s in structures], dtype=np.int32)
+        posn = np.ascontiguousarray(np.concatenate([np.asarray(s.posn, np.float64) for s in structures]))
+        types = np.ascontiguousarray(np.concatenate([np.asarray(s.species, np.int32) for s in structures]))
+        cells = np.ascontiguousarray(np.concatenate([np.asarray(s.cell, np.float64).T.ravel() for s in structures]))
+        eref = np.ascontiguousarray(energy_ref, dtype=np.float64)
+        fref = np.ascontiguousarray(np.concatenate([np.asarray(f, np.float64) for f in force_ref]))
+        err = np.zeros(3)
+        grad = np.zeros(sum(lib().oracle_nnp_nparams(self._h, t) for t in range(self.ntypes)))
+        rc = lib().oracle_train_force_grad(self._h, len(natoms), _ptr(natoms), _ptr(posn), _ptr(types), _ptr(cells), _ptr(eref),
+                                           _ptr(fref), float(beta), int(loss), float(delta), _ptr(err), _ptr(grad))
+        if rc != 0:
+            raise RuntimeError("oracle_train_force_grad failed (%d)" % rc)
+        return err[0], err[1], err[2], grad
 
     def network(self, t, g):
         g = np.ascontiguousarray(g, dtype=np.float64)

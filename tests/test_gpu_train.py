@@ -1,8 +1,9 @@
-"""The energy trainer's batch error and parameter gradient on the GPU (nnpgpu_train_grad) against
-the FP64 oracle (NNPTE::error, src/nnp/nnpte.cpp:870-921, with Cost::grad, src/ml/nn.cpp:1554-1589;
-the oracle's gradient is itself checked against finite differences in tests/test_oracle.py).
-Tolerances: losses 1e-5 relative; gradient 1e-4 of its largest component (FP32 descriptors and
-networks on the GPU)."""
+"""The trainers' batch error and parameter gradient on the GPU against the FP64 oracle: the energy
+trainer (nnpgpu_train_grad; NNPTE::error, src/nnp/nnpte.cpp:870-921, with Cost::grad,
+src/ml/nn.cpp:1554-1589) and the force trainer's loss (nnpgpu_train_force_grad; NNPTEF::error,
+src/nnp/nnptef.cpp:1043-1135).  The oracle's gradients are themselves checked against finite
+differences in tests/test_oracle.py.  Tolerances: losses 1e-5 relative; gradient 1e-4 (energy) and
+2e-4 (with forces: FP32 second derivatives) of its largest component."""
 import os
 
 import numpy as np
@@ -56,3 +57,52 @@ def test_train_grad_rejects_bad_loss(pair):
     s = W.make_structures("mixed512", seed=73, count=1, sizes=[30])
     with pytest.raises(engine.NNPGPUError):
         eng.train_grad(s, np.zeros(1), "HUBER", delta=0.0)
+
+
+# ---- the force trainer (nnpgpu_train_force_grad): loss of NNPTEF::error (nnptef.cpp:1043-1135),
+# exact gradient (the oracle's is checked against finite differences in tests/test_oracle.py)
+def _force_batch(orc, seed, sizes):
+    strucs = W.make_structures("mixed512", seed=seed, count=len(sizes), sizes=sizes)
+    ref = [orc.compute(s.posn, s.species, s.cell, force=True) for s in strucs]
+    rng = np.random.default_rng(seed)
+    eref = np.array([r[0] for r in ref]) + rng.normal(0.0, 0.3, size=len(strucs)) * np.array([s.natoms for s in strucs]) ** 0.5
+    fref = [r[1] + rng.normal(0.0, 0.2, r[1].shape) for r in ref]
+    return strucs, eref, fref
+
+
+@pytest.mark.parametrize("loss,delta", [("MSE", 1.0), ("HUBER", 0.05)])
+def test_train_force_grad_matches_oracle(pair, loss, delta):
+    eng, orc = pair
+    strucs, eref, fref = _force_batch(orc, 81, [16, 40, 120, 300, 600])
+    codes = {"MSE": 0, "MAE": 1, "HUBER": 2, "ASINH": 3}
+    beta = 2.0
+    L, r2, f2, g = eng.train_force_grad(strucs, eref, fref, beta, loss, delta)
+    Lo, r2o, f2o, go = orc.train_force_grad(strucs, eref, fref, beta, codes[loss], delta)
+    assert abs(L - Lo) <= 1e-5 * abs(Lo) + 1e-9
+    assert abs(r2 - r2o) <= 1e-5 * abs(r2o) + 1e-9
+    assert abs(f2 - f2o) <= 1e-5 * abs(f2o) + 1e-9
+    assert np.abs(g - go).max() <= 2e-4 * np.abs(go).max(), np.abs(g - go).max() / np.abs(go).max()
+
+
+def test_train_force_grad_reduces_to_energy_gradient(pair):
+    """beta = 0 leaves the energy trainer's gradient; repeated calls are bit-identical."""
+    eng, orc = pair
+    strucs, eref, fref = _force_batch(orc, 82, [30, 200, 900])
+    L, r2, f2, g = eng.train_force_grad(strucs, eref, fref, 0.0, "MSE")
+    Le, r2e, ge = eng.train_grad(strucs, eref, "MSE")
+    assert L == Le and r2 == r2e and f2 > 0
+    np.testing.assert_array_equal(g, ge)
+    a = eng.train_force_grad(strucs, eref, fref, 1.5, "MSE")
+    b = eng.train_force_grad(strucs, eref, fref, 1.5, "MSE")
+    assert a[:3] == b[:3]
+    np.testing.assert_array_equal(a[3], b[3])
+
+
+def test_train_force_grad_rejects_bad_input(pair):
+    from atomnn_gb300 import engine
+    eng, orc = pair
+    strucs, eref, fref = _force_batch(orc, 83, [20])
+    with pytest.raises(engine.NNPGPUError):
+        eng.train_force_grad(strucs, eref, fref, -1.0, "MSE")
+    with pytest.raises(engine.NNPGPUError):
+        eng.train_force_grad(strucs, eref, fref, 1.0, "ASINH", delta=0.0)

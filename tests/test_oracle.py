@@ -229,3 +229,43 @@ def test_train_gradient_matches_finite_differences(oracle_lib, tmp_path, loss, d
                 vals.append(oracle_lib.OracleNNP(path).train_grad(strucs, eref, loss, delta)[0])
             fd = (vals[0] - vals[1]) / (2 * h)
             assert abs(fd - grad[off + q]) <= 1e-6 + 1e-4 * abs(fd), (t, q, kind, fd, grad[off + q])
+
+
+@pytest.mark.parametrize("loss", [0, 2])
+def test_force_train_gradient_matches_finite_differences(oracle_lib, tmp_path, loss):
+    """The force trainer's batch gradient (energy term plus the force term through the networks'
+    mixed second derivative) equals central differences of its batch loss (nnptef.cpp:1043-1135)
+    in single network parameters of every layer, on small periodic cells whose forces carry the
+    minimum-image rule."""
+    pot = W.make_potential("mixed512")
+    path = str(tmp_path / "p.nnp")
+    W.write_potential(pot, path)
+    strucs = W.make_structures("mixed512", seed=63, count=3, sizes=[10, 18, 14])
+    orc = oracle_lib.OracleNNP(path)
+    ref = [orc.compute(s.posn, s.species, s.cell, force=True) for s in strucs]
+    rng = np.random.default_rng(4)
+    eref = np.array([r[0] for r in ref]) + np.array([0.4, -0.9, 1.3])
+    fref = [r[1] + rng.normal(0.0, 0.3, r[1].shape) for r in ref]
+    beta = 2.5
+    L0, r2, f2, grad = orc.train_force_grad(strucs, eref, fref, beta, loss, 0.05)
+    assert f2 > 0 and r2 > 0
+    h = 1e-6
+    off = 0
+    for t in (0, 1):
+        p0 = orc.params(t)
+        net = pot.nets[t]
+        nb = sum(net.nodes)
+        w0 = nb                                  # first layer-0 weight
+        w1 = nb + net.nin * net.nodes[0]         # first layer-1 weight
+        wl = p0.size - 1                         # last output weight
+        for q in [0, net.nodes[0] + 3, nb - 1, w0 + 7, w0 + 5 * net.nodes[0] + 2, w1 + 11, wl]:
+            vals = []
+            for sgn in (1, -1):
+                p = p0.copy()
+                p[q] += sgn * h
+                orc.set_params(t, p)
+                vals.append(orc.train_force_grad(strucs, eref, fref, beta, loss, 0.05)[0])
+            orc.set_params(t, p0)
+            fd = (vals[0] - vals[1]) / (2 * h)
+            assert abs(fd - grad[off + q]) <= 1e-7 + 1e-5 * abs(fd), (t, q, fd, grad[off + q])
+        off += p0.size
