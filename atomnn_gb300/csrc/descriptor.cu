@@ -367,22 +367,27 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   const int n = min(nb_cnt[i], cap);
-  // neighbour types, one chunk of 32 slots per register (cap <= 32 * QMAX)
+  // neighbour types and vectors, one chunk of 32 slots per register (cap <= 32 * QMAX), all
+  // loads issued before the first ballot consumes one
   int tq[QMAX];
+  float4 rq[QMAX];
+#pragma unroll
+  for (int q = 0; q < QMAX; ++q) {
+    const int s = q * 32 + lane;
+    const size_t g = (size_t)i * cap + s;
+    const bool on = s < n;
+    tq[q] = on ? clamp_type(nb_t ? (int)nb_t[g] : type[nb_j[g]], ntypes) : -1;
+    rq[q] = on ? nb_r[g] : make_float4(0.f, 0.f, 0.f, 1.f);
+  }
   int cnt[NT_MAX];
 #pragma unroll
   for (int t = 0; t < NT_MAX; ++t) cnt[t] = 0;
 #pragma unroll
-  for (int q = 0; q < QMAX; ++q) {
-    const int s = q * 32 + lane;
-    tq[q] = -1;
+  for (int q = 0; q < QMAX; ++q)
     if (q * 32 < n) {
-      const size_t g = (size_t)i * cap + s;
-      tq[q] = (s < n) ? clamp_type(nb_t ? (int)nb_t[g] : type[nb_j[g]], ntypes) : -1;
 #pragma unroll
       for (int tt = 0; tt < NT_MAX; ++tt) cnt[tt] += __popc(__ballot_sync(0xffffffffu, tq[q] == tt));
     }
-  }
   int run[NT_MAX];
   int acc = 0;
 #pragma unroll
@@ -396,7 +401,6 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
   for (int q = 0; q < QMAX; ++q) {
     if (q * 32 >= n) break;
     const int s = q * 32 + lane;
-    const size_t g = (size_t)i * cap + s;
     const int t = tq[q];
     int pos = 0;
 #pragma unroll
@@ -406,7 +410,7 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
       run[tt] += __popc(m);
     }
     if (s < n) {
-      const float4 r = nb_r[g];
+      const float4 r = rq[q];
       const float inv = 1.0f / r.w;
       S.ux[pos] = r.x * inv;
       S.uy[pos] = r.y * inv;
@@ -1018,7 +1022,8 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   const bool cc = cutoff_cache(S, P, I, n);
   const float* gi = dEdG + (size_t)i * gstride;
 
-  // ---- radial chain rule: W_p = BasisR::force(d) * u_p (basis_radial.cpp:371-380, nnp.cpp:441-446)
+  // ---- radial chain rule: W_p = BasisR::force(d) * u_p (basis_radial.cpp:371-380, nnp.cpp:441-446);
+  // functions in groups of four (independent exponentials in flight), GAUSSIAN inline
   for (int J = 0; J < P.ntypes; ++J) {
     const RadialP& R = P.rad[I][J];
     const float* __restrict__ sJ = gi + R.off;
@@ -1032,8 +1037,23 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
         cutoff_fg(R.cut, d, R.rc, R.pirc, R.rci, fc, gc);
       }
       float amp = 0.f;
+      if (R.phi == RAD_GAUSSIAN) {
 #pragma unroll 1
-      for (int f = 0; f < R.n; ++f) amp -= sJ[f] * radial_force_term(R.phi, R.eta[f], R.rs[f], d, fc, gc);
+        for (int f0 = 0; f0 < R.n; f0 += 4) {
+          float t[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int f = min(f0 + k, R.n - 1);
+            const float eta = R.eta[f], x = d - R.rs[f];
+            const float w = (f0 + k < R.n) ? sJ[f] : 0.f;
+            t[k] = w * __expf(-eta * x * x) * fmaf(-2.0f * eta * x, fc, gc);
+          }
+          amp -= (t[0] + t[1]) + (t[2] + t[3]);
+        }
+      } else {
+#pragma unroll 1
+        for (int f = 0; f < R.n; ++f) amp -= sJ[f] * radial_force_term(R.phi, R.eta[f], R.rs[f], d, fc, gc);
+      }
       amp *= R.norm;
       S.wx[p] = amp * S.ux[p];
       S.wy[p] = amp * S.uy[p];
