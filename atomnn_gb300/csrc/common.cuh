@@ -17,7 +17,7 @@ constexpr int NIN_MAX = 256;                       // network inputs
 constexpr int MOM_N = 4;                           // largest zeta of a moment-tensor block
 constexpr int MOM_C = 35;                          // symmetric tensor components of degree 0..MOM_N
 constexpr int MOM_Q = 20;                          // components of degree 0..MOM_N-1
-constexpr int MOM_EX = 8 * MOM_Q;                  // per-width floats a moment block needs in shared memory
+constexpr int MOM_EX = 8 * MOM_Q + 2 * MOM_C + 2;  // per-width floats a moment block needs in shared memory
 constexpr int NLAYER_MAX = 4;                      // network layers (hidden + output)
 constexpr int HID_MAX = 256;                       // nodes per layer
 
@@ -43,12 +43,15 @@ struct RadialP {
 // (e*NL + l)*NZ_MAX + m of file function f.  phi is the radial factor (ANG_*): GAUSS, IPOWP and
 // SECHP are products h(r_ij) h(r_ik), IPOWS and SECHS functions of r_ij^alpha + r_ik^alpha.
 // mom = 1 marks a block evaluated through moment tensors (a product family, every zeta <= 4,
-// |lambda| <= 1); its moments start at float moff of the atom's row.
+// |lambda| <= 1); its moments start at float moff of the atom's row.  tab is the block's offset
+// in PotParams::atab: n grid cells (as floats), then for a moment block the n x (ne*(MOM_N+1))
+// matrix M[f][e*(MOM_N+1)+k] = norm * (coefficient of cos^k in function f's angular term) when f
+// has width e, 0 otherwise.
 struct AngP {
   int n, off, cut, alpha;
   float rc, pirc, rci, norm;
   int ne, nl, nz, mom;
-  int moff, phi, pad1, pad2;
+  int moff, phi, tab, pad2;
   float ietap[NE_MAX];
   float lam[NL];
   signed char gidx[NA_MAX];
@@ -62,6 +65,7 @@ struct PotParams {
   int kx;       // 1: a triplet-path block of IPOWP or SECHP needs per-pair derivative weights
   int gen;      // 1: some angular block has a family other than GAUSS
   int pad;
+  const float* atab;  // per-block tables of the angular functions (AngP::tab), device memory
   // cutoff shared by every basis of centre type I (ccut 0: the bases differ)
   int ccut[NT_MAX];
   float crc[NT_MAX], cpirc[NT_MAX], crci[NT_MAX];

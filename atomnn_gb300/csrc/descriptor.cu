@@ -25,16 +25,18 @@ namespace nnpgpu {
 constexpr int QMAX = 8;  // owner chunks of 32 per block -> at most 256 neighbours
 
 struct WarpSmem {
-  float *ux, *uy, *uz, *d, *inv, *fc, *gc, *dpa, *ex, *kx, *wx, *wy, *wz, *scratch;
+  float *ux, *uy, *uz, *d, *inv, *fc, *gc, *dpa, *ex, *kx, *wx, *wy, *wz, *scratch, *gi;
   int *orig, *toff;
 };
 
 // The per-width region ex is at least MOM_EX floats per width so that a moment block's tensors
-// (two sets of MOM_C per width plus the diagonal terms) fit there.  With kx, a second per-width
+// fit there: in the descriptor pass two sets of MOM_C per width plus the diagonal terms, in the
+// chain rule two contraction tables of MOM_Q float4 per width followed by the stored moments.  With kx, a second per-width
 // region holds the pair factors' derivative weights (IPOWP and SECHP blocks of the force pass).
+// ng floats at the end hold the centre's dE/dG row in the force pass (0 elsewhere).
 __host__ __device__ inline int ex_stride(int cap) { return cap > MOM_EX ? cap : MOM_EX; }
-__host__ __device__ inline size_t warp_smem_floats(int cap, int ne, bool kx) {
-  return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + (kx ? (size_t)ne * cap : 0) + 64 + 8;
+__host__ __device__ inline size_t warp_smem_floats(int cap, int ne, bool kx, int ng = 0) {
+  return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + (kx ? (size_t)ne * cap : 0) + 64 + 8 + ng;
 }
 
 __device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
@@ -48,6 +50,7 @@ __device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
   s.orig = reinterpret_cast<int*>(w + 3 * cap);
   s.scratch = w + 4 * cap;
   s.toff = reinterpret_cast<int*>(s.scratch + 64);
+  s.gi = s.scratch + 72;
   return s;
 }
 
@@ -93,8 +96,6 @@ __device__ const signed char c_mom_up[MOM_Q][3] = {{1, 2, 3},    {4, 5, 6},    {
                                                    {11, 13, 14}, {12, 14, 15}, {13, 16, 17}, {14, 17, 18}, {15, 18, 19},
                                                    {20, 21, 22}, {21, 23, 24}, {22, 24, 25}, {23, 26, 27}, {24, 27, 28},
                                                    {25, 28, 29}, {26, 30, 31}, {27, 31, 32}, {28, 32, 33}, {29, 33, 34}};
-// binomial(zeta, n) / 2^zeta for zeta = 1, 2, 4
-__device__ const float c_mom_binom[3][MOM_N + 1] = {{0.5f, 0.5f, 0, 0, 0}, {0.25f, 0.5f, 0.25f, 0, 0}, {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f}};
 
 // Moments of nsets slot ranges (set 0: [lo0,hi0), set 1: [lo1,hi1)) for every width of the block:
 // M[(set*ne + e)*MOM_C + r] = sum over the set's slots of w_e u^(a,b,c).  Each (set, width) pair
@@ -174,17 +175,11 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nse
   }
 }
 
-// coefficient of cos^n in ((1 + lam cos)/2)^zeta, zeta = 2^m <= 4: binomial / 2^zeta * lam^n
-__device__ __forceinline__ float mom_coef(int m, float lam, int n) {
-  float lp = 1.f;
-  for (int k = 0; k < n; ++k) lp *= lam;
-  return c_mom_binom[m][n] * lp;
-}
 
 // G4 of a moment block (BasisA::symm summed as in NNP::symm, nnp.cpp:359-377)
 template <bool GEN>
-__device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool same, int j0, int nJ, int k0, int nK, float* __restrict__ gmom,
-                               float* __restrict__ Gi) {
+__device__ void symm_mom_block(const WarpSmem& S, const AngP& A, const float* __restrict__ atab, bool cc, bool same, int j0, int nJ, int k0,
+                               int nK, float* __restrict__ gmom, float* __restrict__ Gi) {
   const int lane = threadIdx.x & 31;
   const int nec = A.ne * MOM_C;
   float* MJ = S.ex;
@@ -208,16 +203,13 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool s
     V[lane] = s;
   }
   __syncwarp();
+  // G_f = sum_k M[f][k] V[k] (the block's coefficient matrix, norm included)
+  const int w = A.ne * (MOM_N + 1);
+  const float* __restrict__ M = atab + A.tab + A.n;
   for (int f = lane; f < A.n; f += 32) {
-    const int cell = A.gidx[f];
-    const int e = cell / (NL * NZ_MAX), m = cell % NZ_MAX, zeta = 1 << m;
-    const float lam = A.lam[(cell / NZ_MAX) % NL];
-    float v = 0.f, lp = 1.f;
-    for (int n = 0; n <= zeta; ++n) {
-      v = fmaf(c_mom_binom[m][n] * lp, V[e * (MOM_N + 1) + n], v);
-      lp *= lam;
-    }
-    Gi[A.off + f] = A.norm * v;
+    float v = 0.f;
+    for (int k = 0; k < w; ++k) v = fmaf(M[f * w + k], V[k], v);
+    Gi[A.off + f] = v;
   }
   __syncwarp();
 }
@@ -318,35 +310,57 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
 
 // chain rule of a moment block (BasisA::force summed as in NNP::force, nnp.cpp:466-478)
 template <bool GEN>
-__device__ void force_mom_block(const WarpSmem& S, const AngP& A, bool cc, bool same, int j0, int nJ, int k0, int nK,
-                                const float* __restrict__ gmom, const float* __restrict__ gi) {
+__device__ void force_mom_block(const WarpSmem& S, const AngP& A, const float* __restrict__ atab, bool cc, bool same, int j0, int nJ, int k0,
+                                int nK, const float* __restrict__ gmom, const float* __restrict__ gi) {
   const int lane = threadIdx.x & 31;
   const int nec = A.ne * MOM_C;
-  // b[e][n] = norm * sum over the block's functions of width e of dE/dG_f * coef_n(f)
+  // b[e][n] = norm * sum over the block's functions of width e of dE/dG_f * coef_n(f): the block's
+  // coefficient matrix applied to the dE/dG values (lanes over its columns, rows coalesced)
   float* b = S.scratch;
   float* T0 = S.scratch + 32;  // [set][e]
-  if (lane < A.ne * (MOM_N + 1)) {
-    const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
-    float s = 0.f;
-    for (int f = 0; f < A.n; ++f) {
-      const int cell = A.gidx[f];
-      if (cell / (NL * NZ_MAX) != e) continue;
-      if (n <= (1 << (cell % NZ_MAX))) s = fmaf(gi[A.off + f], mom_coef(cell % NZ_MAX, A.lam[(cell / NZ_MAX) % NL], n), s);
+  {
+    const int w = A.ne * (MOM_N + 1);
+    const float* __restrict__ M = atab + A.tab + A.n;
+    if (lane < w) {
+      float s0 = 0.f, s1 = 0.f;
+      int f = 0;
+      for (; f + 1 < A.n; f += 2) {
+        s0 = fmaf(gi[A.off + f], M[f * w + lane], s0);
+        s1 = fmaf(gi[A.off + f + 1], M[(f + 1) * w + lane], s1);
+      }
+      if (f < A.n) s0 = fmaf(gi[A.off + f], M[f * w + lane], s0);
+      b[lane] = s0 + s1;
     }
-    b[lane] = A.norm * s;
   }
   __syncwarp();
   // the contraction tables of each set: b_(deg q + 1) times the three components one degree up
   float4* TJ = reinterpret_cast<float4*>(S.ex);
   float4* TK = same ? TJ : TJ + A.ne * MOM_Q;
   const int nsets = same ? 1 : 2;
-  for (int t = lane; t < nsets * A.ne * MOM_Q; t += 32) {
+  const int nt = nsets * A.ne * MOM_Q;
+  // the stored moments, copied coalesced into the region after the tables (all loads in flight
+  // at once), then the tables built from shared memory
+  float* raw = S.ex + 8 * A.ne * MOM_Q;
+  constexpr int RR = (2 * NE_MAX * MOM_C + 31) / 32;
+  float rv[RR];
+#pragma unroll
+  for (int r = 0; r < RR; ++r) {
+    const int k = lane + 32 * r;
+    rv[r] = k < nsets * nec ? gmom[k] : 0.f;
+  }
+#pragma unroll
+  for (int r = 0; r < RR; ++r) {
+    const int k = lane + 32 * r;
+    if (k < nsets * nec) raw[k] = rv[r];
+  }
+  __syncwarp();
+  for (int t = lane; t < nt; t += 32) {
     const int set = t / (A.ne * MOM_Q), e = (t / MOM_Q) % A.ne, q = t % MOM_Q;
     const float bn = b[e * (MOM_N + 1) + mom_deg(q) + 1];
-    const float* Mg = gmom + set * nec + e * MOM_C;
+    const float* Mg = raw + set * nec + e * MOM_C;
     (set ? TK : TJ)[e * MOM_Q + q] = make_float4(bn * Mg[c_mom_up[q][0]], bn * Mg[c_mom_up[q][1]], bn * Mg[c_mom_up[q][2]], 0.f);
   }
-  if (lane < nsets * A.ne) T0[lane] = b[(lane % A.ne) * (MOM_N + 1)] * gmom[(lane / A.ne) * nec + (lane % A.ne) * MOM_C];
+  if (lane < nsets * A.ne) T0[lane] = b[(lane % A.ne) * (MOM_N + 1)] * raw[(lane / A.ne) * nec + (lane % A.ne) * MOM_C];
   __syncwarp();
   // J's slots against the K moments (J's own for J == K); K's slots against the J moments
   if (!GEN || A.phi == ANG_GAUSS) {
@@ -991,7 +1005,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (A.mom) {
-        symm_mom_block<GEN>(S, A, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
+        symm_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
         continue;
       }
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, true);
@@ -999,7 +1013,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       __syncwarp();
       run_block<false, NEK, NZK, GEN>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
-      for (int f = lane; f < A.n; f += 32) Gi[A.off + f] = A.norm * S.scratch[A.gidx[f]];
+      for (int f = lane; f < A.n; f += 32) Gi[A.off + f] = A.norm * S.scratch[(int)P.atab[A.tab + f]];
       __syncwarp();
     }
 }
@@ -1016,11 +1030,13 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
   const bool kx = GEN && P.kx;  // a compile-time false in the GAUSS-only instances
-  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, kx), cap, NEK, kx);
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, kx, gstride), cap, NEK, kx);
   const int I = clamp_type(type[i], P.ntypes);
+  // the centre's dE/dG row into shared memory: every block reads it several times
+  for (int k = lane; k < P.nin[I]; k += 32) S.gi[k] = dEdG[(size_t)i * gstride + k];
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
   const bool cc = cutoff_cache(S, P, I, n);
-  const float* gi = dEdG + (size_t)i * gstride;
+  const float* gi = S.gi;
 
   // ---- radial chain rule: W_p = BasisR::force(d) * u_p (basis_radial.cpp:371-380, nnp.cpp:441-446);
   // functions in groups of four (independent exponentials in flight), GAUSSIAN inline
@@ -1071,15 +1087,17 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
       if (A.mom) {
-        force_mom_block<GEN>(S, A, cc, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
+        force_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
         continue;
       }
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, false);
       if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, false);
-      // dE/dG on the function grid (duplicates of a grid cell add up)
-      if (lane == 0) {
-        for (int c = 0; c < NE_MAX * NL * NZ_MAX; ++c) S.scratch[c] = 0.f;
-        for (int f = 0; f < A.n; ++f) S.scratch[A.gidx[f]] += gi[A.off + f];
+      // dE/dG on the function grid, one lane per grid cell (duplicates of a cell add up in file order)
+      for (int c = lane; c < NE_MAX * NL * NZ_MAX; c += 32) {
+        float v = 0.f;
+        for (int f = 0; f < A.n; ++f)
+          if (A.gidx[f] == c) v += gi[A.off + f];
+        S.scratch[c] = v;
       }
       __syncwarp();
       run_block<true, NEK, NZK, GEN>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
@@ -1246,7 +1264,7 @@ __global__ void __launch_bounds__(128) tangent_kernel(const __grid_constant__ Po
       __syncwarp();
       tangent_block<NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
-      for (int f = lane; f < A.n; f += 32) Ui[A.off + f] = -A.norm * S.scratch[A.gidx[f]];
+      for (int f = lane; f < A.n; f += 32) Ui[A.off + f] = -A.norm * S.scratch[(int)P.atab[A.tab + f]];
       __syncwarp();
     }
 }
@@ -1273,7 +1291,7 @@ int launch_tangent(const BatchDev& B, const PotParams& P, int ne, int nz, const 
 }
 
 size_t symm_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne, false) * warps; }
-size_t force_smem_bytes(int cap, int ne, int warps, bool kx) { return sizeof(float) * warp_smem_floats(cap, ne, kx) * warps; }
+size_t force_smem_bytes(int cap, int ne, int warps, bool kx, int gstride) { return sizeof(float) * warp_smem_floats(cap, ne, kx, gstride) * warps; }
 
 template <int NEK, int NZK, bool GEN>
 static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
@@ -1286,7 +1304,7 @@ template <int NEK, int NZK, bool GEN>
 static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  force_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps, GEN && P.kx), st>>>(
+  force_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps, GEN && P.kx, B.gstride), st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
 }
 

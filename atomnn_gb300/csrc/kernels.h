@@ -70,7 +70,7 @@ void launch_reverse(const BatchDev& B, cudaStream_t st);
 int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
 int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
 size_t symm_smem_bytes(int cap, int ne, int warps);
-size_t force_smem_bytes(int cap, int ne, int warps, bool kx);
+size_t force_smem_bytes(int cap, int ne, int warps, bool kx, int gstride);
 // atomic networks: FP32 SIMT path and BF16 tensor-core path
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st);
 size_t type_sort_ints(int natoms);  // ints of the type_count buffer for a batch of natoms

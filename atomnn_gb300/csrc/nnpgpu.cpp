@@ -547,6 +547,7 @@ extern "C" int nnpgpu_create(const char* potfile, const nnpgpu_opts* opts, nnpgp
     push(std::vector<float>(n.inpw.begin(), n.inpw.end()));
     push(std::vector<float>(n.inpb.begin(), n.inpb.end()));
   }
+  push(build_ang_tables(c->pot, c->P));
   c->netbytes = host.size() * sizeof(float);
   if (cudaMalloc(&c->netbuf, c->netbytes) != cudaSuccess) {
     cudaGetLastError();
@@ -575,6 +576,7 @@ extern "C" int nnpgpu_create(const char* potfile, const nnpgpu_opts* opts, nnpgp
     p.outb = (float)n.outb[0];
     p.evac = c->pot.types[t].energy;
   }
+  c->P.atab = base + offs[k++];
   prepare_tc_weights(c);
   *out = c;
   return NNPGPU_OK;

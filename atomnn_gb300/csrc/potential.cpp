@@ -331,4 +331,37 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
   }
 }
 
+std::vector<float> build_ang_tables(const HPot& pot, PotParams& P) {
+  std::vector<float> tab;
+  for (int I = 0; I < pot.ntypes; ++I)
+    for (int q = 0; q < pot.ntypes * (pot.ntypes + 1) / 2; ++q) {
+      AngP& a = P.ang[I][q];
+      if (a.n == 0) continue;
+      while (tab.size() % 4) tab.push_back(0.f);
+      a.tab = (int)tab.size();
+      for (int f = 0; f < a.n; ++f) tab.push_back((float)a.gidx[f]);
+      if (!a.mom) continue;
+      const HBasisA& b = pot.ang[I][q];
+      const int w = a.ne * (MOM_N + 1);
+      const double norm = norm_value(b.norm, b.rc);
+      for (int f = 0; f < a.n; ++f) {
+        const int cell = a.gidx[f];
+        const int e = cell / (NL * NZ_MAX), m = cell % NZ_MAX, zeta = 1 << m;
+        const double lam = a.lam[(cell / NZ_MAX) % NL];
+        // ((1 + lam c)/2)^zeta = sum_k binom(zeta, k) / 2^zeta lam^k c^k
+        for (int col = 0; col < w; ++col) {
+          const int ce = col / (MOM_N + 1), k = col % (MOM_N + 1);
+          double v = 0.0;
+          if (ce == e && k <= zeta) {
+            double binom = 1.0;
+            for (int j = 0; j < k; ++j) binom = binom * (zeta - j) / (j + 1);
+            v = norm * binom * std::pow(lam, k) / (double)(1 << zeta);
+          }
+          tab.push_back((float)v);
+        }
+      }
+    }
+  return tab;
+}
+
 }  // namespace nnpgpu

@@ -51,5 +51,8 @@ struct PotError : std::runtime_error {
 HPot read_potential(const char* path);
 // Fills the kernel tables; throws PotError(NNPGPU_ERR_UNSUPPORTED) for forms the kernels lack.
 void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max);
+// the per-block angular tables (AngP::tab) after build_tables: sets each block's tab offset and
+// returns the floats; P.atab is set by the caller once they are on the device
+std::vector<float> build_ang_tables(const HPot& pot, PotParams& P);
 
 }  // namespace nnpgpu
