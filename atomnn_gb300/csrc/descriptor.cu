@@ -203,12 +203,18 @@ __device__ void symm_mom_block(const WarpSmem& S, const AngP& A, const float* __
     V[lane] = s;
   }
   __syncwarp();
-  // G_f = sum_k M[f][k] V[k] (the block's coefficient matrix, norm included)
+  // G_f = sum_k M[f][k] V[k] (the block's coefficient matrix, norm included), one width at a time
   const int w = A.ne * (MOM_N + 1);
   const float* __restrict__ M = atab + A.tab + A.n;
   for (int f = lane; f < A.n; f += 32) {
     float v = 0.f;
-    for (int k = 0; k < w; ++k) v = fmaf(M[f * w + k], V[k], v);
+    for (int e = 0; e < A.ne; ++e) {
+      float m[MOM_N + 1];
+#pragma unroll
+      for (int k = 0; k <= MOM_N; ++k) m[k] = M[f * w + e * (MOM_N + 1) + k];
+#pragma unroll
+      for (int k = 0; k <= MOM_N; ++k) v = fmaf(m[k], V[e * (MOM_N + 1) + k], v);
+    }
     Gi[A.off + f] = v;
   }
   __syncwarp();
@@ -252,7 +258,7 @@ __device__ void mom_contract(const WarpSmem& S, const AngP& A, bool cc, int lo, 
 #pragma unroll
           for (int bb = n - a; bb >= 0; --bb) {
             const int c = n - a - bb;
-            mono[mom_idx(a, bb, c)] = c_mom_mult[mom_idx(a, bb, c)] * px[a] * (py[bb] * pz[c]);
+            mono[mom_idx(a, bb, c)] = mom_mult(a, bb, c) * px[a] * (py[bb] * pz[c]);
           }
     }
     float gx = 0.f, gy = 0.f, gz = 0.f;
@@ -337,7 +343,6 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, const float* _
   float4* TJ = reinterpret_cast<float4*>(S.ex);
   float4* TK = same ? TJ : TJ + A.ne * MOM_Q;
   const int nsets = same ? 1 : 2;
-  const int nt = nsets * A.ne * MOM_Q;
   // the stored moments, copied coalesced into the region after the tables (all loads in flight
   // at once), then the tables built from shared memory
   float* raw = S.ex + 8 * A.ne * MOM_Q;
@@ -354,11 +359,15 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, const float* _
     if (k < nsets * nec) raw[k] = rv[r];
   }
   __syncwarp();
-  for (int t = lane; t < nt; t += 32) {
-    const int set = t / (A.ne * MOM_Q), e = (t / MOM_Q) % A.ne, q = t % MOM_Q;
-    const float bn = b[e * (MOM_N + 1) + mom_deg(q) + 1];
-    const float* Mg = raw + set * nec + e * MOM_C;
-    (set ? TK : TJ)[e * MOM_Q + q] = make_float4(bn * Mg[c_mom_up[q][0]], bn * Mg[c_mom_up[q][1]], bn * Mg[c_mom_up[q][2]], 0.f);
+  // lane q builds entry q of every (set, width) table: its three component indices are fixed
+  if (lane < MOM_Q) {
+    const int u0 = c_mom_up[lane][0], u1 = c_mom_up[lane][1], u2 = c_mom_up[lane][2], dq = mom_deg(lane) + 1;
+    for (int se = 0; se < nsets * A.ne; ++se) {
+      const int set = se / A.ne, e = se % A.ne;
+      const float bn = b[e * (MOM_N + 1) + dq];
+      const float* Mg = raw + set * nec + e * MOM_C;
+      (set ? TK : TJ)[e * MOM_Q + lane] = make_float4(bn * Mg[u0], bn * Mg[u1], bn * Mg[u2], 0.f);
+    }
   }
   if (lane < nsets * A.ne) T0[lane] = b[(lane % A.ne) * (MOM_N + 1)] * raw[(lane / A.ne) * nec + (lane % A.ne) * MOM_C];
   __syncwarp();
