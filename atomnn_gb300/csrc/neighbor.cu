@@ -107,18 +107,23 @@ __global__ void __launch_bounds__(256) cell_scan_kernel(int s0, const StrucMeta*
   if (threadIdx.x == 0) cell_start[S.cell0 + ncell] = carry;
 }
 
-// Places each atom of a cell-list structure into its cell.  The count is taken back down to
-// zero on the way, so the counts are clean for the next call.  The order within a cell does
-// not matter: the neighbour kernel sorts every list by neighbour index.
+// Places each atom of a cell-list structure into its cell, with cell-ordered copies of its
+// wrapped coordinates and floors (the candidates of a stencil run are then contiguous in
+// memory).  The count is taken back down to zero on the way, so the counts are clean for the
+// next call.  The order within a cell does not matter: the neighbour kernel sorts every list by
+// neighbour index.
 __global__ void cell_fill_kernel(int a0, int natoms, const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
                                  const int* __restrict__ atom_cell, int* __restrict__ cell_cnt, const int* __restrict__ cell_start,
-                                 int* __restrict__ cell_atoms) {
+                                 int* __restrict__ cell_atoms, const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
+                                 float4* __restrict__ sfrac_c, int4* __restrict__ sfloor_c) {
   const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a0 + natoms) return;
   if (meta[atom_struc[i]].mode != 4) return;
   const int c = atom_cell[i];
   const int pos = cell_start[c] + atomicSub(&cell_cnt[c], 1) - 1;
   cell_atoms[pos] = i;
+  sfrac_c[pos] = sfrac[i];
+  sfloor_c[pos] = sfloor[i];
 }
 
 __device__ __forceinline__ void emit(int slot, int cap, int j, float rx, float ry, float rz, float dr, int code,
@@ -186,9 +191,10 @@ __device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& 
 // Single-image decision (modes 2 and 4) for centre i and candidate j: the Cell::diff image of
 // j is kept when |diff|^2 <= rc^2.  FP32 from the wrapped fractional coordinates, with the FP64
 // replay of Cell::diff when |diff|^2 lies within the margin of rc^2.
-// sj = sfrac[j], loaded by the caller ahead of use.
+// sj = the candidate's wrapped coordinates, loaded by the caller ahead of use; its floors are
+// sfl[jf] (the atom's own entry, or its cell-ordered copy).
 __device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& si, const int4& fi, int j, const float4 sj,
-                                             const int4* __restrict__ sfloor, const double* __restrict__ posn, double pi0, double pi1,
+                                             const int4* __restrict__ sfl, int jf, const double* __restrict__ posn, double pi0, double pi1,
                                              double pi2, double rc2, float rc2f, float m, float& r0, float& r1, float& r2, float& dr,
                                              int D[3]) {
   const float dl0 = si.x - sj.x, dl1 = si.y - sj.y, dl2 = si.z - sj.z;
@@ -197,7 +203,7 @@ __device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& s
   rf_mul(S, dl0 - q0, dl1 - q1, dl2 - q2, r0, r1, r2);
   const float d2f = r0 * r0 + r1 * r1 + r2 * r2;
   if (d2f > rc2f + m) return false;
-  const int4 fj = sfloor[j];
+  const int4 fj = sfl[jf];
   D[0] = k0 + fi.x - fj.x;
   D[1] = k1 + fi.y - fj.y;
   D[2] = k2 + fi.z - fj.z;
@@ -227,13 +233,17 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
                                                        const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
                                                        const ImgEntry* __restrict__ imgs, const int* __restrict__ atom_cell,
                                                        const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
+                                                       const float4* __restrict__ sfrac_c, const int4* __restrict__ sfloor_c,
                                                        int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
                                                        unsigned char* __restrict__ nb_t, int* __restrict__ nb_cnt,
                                                        int* __restrict__ status) {
   const int lane = threadIdx.x & 31;
-  const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
   const StrucMeta& S = meta[atom_struc[i]];
+  // cell-list centres in cell order: the warps of a CTA (and of an SM) then search overlapping
+  // stencils and share the candidates' lines in L1
+  if (S.mode == 4) i = cell_atoms[i];
   const double rc2 = rc * rc;
   const float rc2f = (float)rc2, m = S.margin;
   const int j0 = S.atom0, nj = S.natoms;
@@ -258,7 +268,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       bool keep = false;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       int D[3] = {0, 0, 0};
-      if (jl < nj && j != i) keep = single_image(S, si, fi, j, sj, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
+      if (jl < nj && j != i) keep = single_image(S, si, fi, j, sj, sfloor, j, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       if (keep) emit(count + __popc(mk & lt), cap, j, r0, r1, r2, dr, pack_code(D[0], D[1], D[2], true), oj, orr, oc, ot, sfrac);
       count += __popc(mk);
@@ -330,7 +340,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
     __syncwarp();
     const float4 si = sfrac[i];
     const int4 fi = sfloor[i];
-    // candidate qd -> atom: last range with prefix <= qd, then its slice of cell_atoms
+    // candidate qd -> its position in cell_atoms: last range with prefix <= qd, then its slice
     auto candidate = [&](int qd) -> int {
       int lo = 0, hi = nr - 1;
       while (lo < hi) {
@@ -338,23 +348,27 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
         if (rp[mid] <= qd) lo = mid;
         else hi = mid - 1;
       }
-      return cell_atoms[rb[lo] + qd - rp[lo]];
+      return rb[lo] + qd - rp[lo];
     };
-    // the next chunk's candidates and coordinates are fetched while this chunk is decided
-    int jn = lane < total ? candidate(lane) : -1;
-    float4 sn = jn >= 0 ? sfrac[jn] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // the next chunk's candidates and coordinates are fetched while this chunk is decided; the
+    // coordinates come from the cell-ordered copy (contiguous along a run)
+    int pn = lane < total ? candidate(lane) : -1;
+    int jn = pn >= 0 ? cell_atoms[pn] : -1;
+    float4 sn = pn >= 0 ? sfrac_c[pn] : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c = 0; c < total; c += 32) {
-      const int j = jn;
+      const int j = jn, pj = pn;
       const float4 sj = sn;
       const int qn = c + 32 + lane;
       if (qn < total) {
-        jn = candidate(qn);
-        sn = sfrac[jn];
+        pn = candidate(qn);
+        jn = cell_atoms[pn];
+        sn = sfrac_c[pn];
       }
       bool keep = false;
       float r0 = 0.f, r1 = 0.f, r2 = 0.f, dr = 0.f;
       int D[3] = {0, 0, 0};
-      if (c + lane < total && j != i) keep = single_image(S, si, fi, j, sj, sfloor, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
+      if (c + lane < total && j != i)
+        keep = single_image(S, si, fi, j, sj, sfloor_c, pj, posn, pi0, pi1, pi2, rc2, rc2f, m, r0, r1, r2, dr, D);
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       const int slot = count + __popc(mk & lt);
       if (keep && slot < cap) {
@@ -630,14 +644,15 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   if (B.ncells > 0) {
     cell_scan_kernel<<<B.nstruc, 256, 0, st>>>(B.s0, B.meta, B.cell_cnt, B.cell_start);
     cell_fill_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.atom_struc, B.meta, B.atom_cell, B.cell_cnt, B.cell_start,
-                                                             B.cell_atoms);
+                                                             B.cell_atoms, B.sfrac, B.sfloor, B.sfrac_c, B.sfloor_c);
     smem = neighbor_smem_bytes(B.cap, warps);
     static bool attr = false;  // skin lists may ask for up to 1024 slots per atom (106 KB)
     if (!attr) attr = cudaFuncSetAttribute(neighbor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   }
   const int blocks = (B.natoms + warps - 1) / warps;
   neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
-                                             B.atom_cell, B.cell_start, B.cell_atoms, B.nb_j, B.nb_r, B.nb_code, B.nb_t, B.nb_cnt, B.status);
+                                             B.atom_cell, B.cell_start, B.cell_atoms, B.sfrac_c, B.sfloor_c, B.nb_j, B.nb_r, B.nb_code, B.nb_t,
+                                             B.nb_cnt, B.status);
 }
 
 void launch_reverse(const BatchDev& B, cudaStream_t st) {

@@ -328,7 +328,8 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
     // cell counts must start at zero: fresh memory is cleared, later calls leave them at zero
     const size_t before = c->cell_cnt.bytes;  // a grown buffer is a new allocation
     ok = ensure(c, c->cell_cnt, sizeof(int) * U.ncells) && ensure(c, c->cell_start, sizeof(int) * U.ncells) &&
-         ensure(c, c->cell_atoms, sizeof(int) * N) && ensure(c, c->atom_cell, sizeof(int) * N);
+         ensure(c, c->cell_atoms, sizeof(int) * N) && ensure(c, c->atom_cell, sizeof(int) * N) &&
+         ensure(c, c->sfrac_c, sizeof(float4) * N) && ensure(c, c->sfloor_c, sizeof(int4) * N);
     if (ok && c->cell_cnt.bytes != before) cudaMemsetAsync(c->cell_cnt.p, 0, c->cell_cnt.bytes, st);
   }
   if (!ok) return set_error(c, NNPGPU_ERR_OOM, "device allocation failed or HBM budget exceeded");
@@ -392,6 +393,8 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
     B.cell_start = (int*)c->cell_start.p;
     B.cell_atoms = (int*)c->cell_atoms.p;
     B.atom_cell = (int*)c->atom_cell.p;
+    B.sfrac_c = (float4*)c->sfrac_c.p;
+    B.sfloor_c = (int4*)c->sfloor_c.p;
   }
   B.orphans = (int*)c->orphans.p;
   B.orphan_cap = std::max(U.natoms, 1);
@@ -590,7 +593,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
                     &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
                     &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
                     &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in, &c->tr_fref, &c->tr_t,
-                    &c->tr_fatom, &c->tr_fstruc, &c->tr_u};
+                    &c->tr_fatom, &c->tr_fstruc, &c->tr_u, &c->sfrac_c, &c->sfloor_c};
   for (DevBuf* b : bufs)
     if (b->p) cudaFree(b->p);
   if (c->netbuf) cudaFree(c->netbuf);
