@@ -5,9 +5,9 @@
 // Here F_j = sum_{s in list(j)} W[j,s] - sum_{s in list(j), min} W[rev(j,s)], where rev is the
 // transposed slot built by reverse_kernel: a gather over the atom's own list, no atomics.
 // Each lane sums its few slots without rounding loss as an unevaluated pair hi + lo of floats
-// (TwoSum, Knuth; the pair carries about 48 bits), and the lanes' pairs are added in FP64.  The
-// FP64 pipe (1/64 of the FP32 rate on GB300) then sees a few operations per atom instead of
-// two per slot and component.
+// (TwoSum, Knuth; the pair carries about 48 bits), the lanes' pairs are added pairwise the same
+// way across the warp, and only the final pair becomes FP64: GB300's FP64 pipe (1/64 of the
+// FP32 rate) sees a handful of operations per atom instead of a warp-wide FP64 reduction.
 #include "common.cuh"
 #include "kernels.h"
 
@@ -27,8 +27,24 @@ struct PairSum {
     hi = s;
     lo = __fadd_rn(lo, e);
   }
+  // adds another pair: TwoSum of the high parts, the low parts and the rounding error summed
+  __device__ __forceinline__ void add_pair(float h, float l) {
+    float s, e;
+    two_sum(hi, h, s, e);
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, l), e);
+  }
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
+// pairwise across the warp; lane 0 ends with the total pair
+__device__ __forceinline__ void warp_pair_sum(PairSum& p) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h = __shfl_down_sync(0xffffffffu, p.hi, o);
+    const float l = __shfl_down_sync(0xffffffffu, p.lo, o);
+    p.add_pair(h, l);
+  }
+}
 
 __global__ void __launch_bounds__(128) gather_kernel(int a0, int natoms, int cap, const int* __restrict__ nb_code,
                                                      const int* __restrict__ nb_cnt, const int* __restrict__ nb_rev,
@@ -54,9 +70,10 @@ __global__ void __launch_bounds__(128) gather_kernel(int a0, int natoms, int cap
       }
     }
   }
-  const double fx = warp_sum_d(sx.value());
-  const double fy = warp_sum_d(sy.value());
-  const double fz = warp_sum_d(sz.value());
+  warp_pair_sum(sx);
+  warp_pair_sum(sy);
+  warp_pair_sum(sz);
+  const double fx = sx.value(), fy = sy.value(), fz = sz.value();
   if (lane == 0) {
     force[3 * (size_t)j] = fx;
     force[3 * (size_t)j + 1] = fy;
