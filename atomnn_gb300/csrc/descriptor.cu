@@ -31,7 +31,7 @@ struct WarpSmem {
 
 // The per-width region ex is at least MOM_EX floats per width so that a moment block's tensors
 // fit there: in the descriptor pass two sets of MOM_C per width plus the diagonal terms, in the
-// chain rule two contraction tables of MOM_Q float4 per width followed by the stored moments.  With kx, a second per-width
+// chain rule two contraction tables of MOM_Q float4 per width.  With kx, a second per-width
 // region holds the pair factors' derivative weights (IPOWP and SECHP blocks of the force pass).
 // ng floats at the end hold the centre's dE/dG row in the force pass (0 elsewhere).
 __host__ __device__ inline int ex_stride(int cap) { return cap > MOM_EX ? cap : MOM_EX; }
@@ -53,6 +53,16 @@ __device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
   s.gi = s.scratch + 72;
   return s;
 }
+
+// Asynchronous 16-byte global -> shared copies (cp.async): the row of a centre is requested at
+// the start of the kernel and waited for where it is first used.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ float powi(float x, int a) {
   float y = 1.f;
@@ -343,22 +353,8 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, const float* _
   float4* TJ = reinterpret_cast<float4*>(S.ex);
   float4* TK = same ? TJ : TJ + A.ne * MOM_Q;
   const int nsets = same ? 1 : 2;
-  // the stored moments, copied coalesced into the region after the tables (all loads in flight
-  // at once), then the tables built from shared memory
-  float* raw = S.ex + 8 * A.ne * MOM_Q;
-  constexpr int RR = (2 * NE_MAX * MOM_C + 31) / 32;
-  float rv[RR];
-#pragma unroll
-  for (int r = 0; r < RR; ++r) {
-    const int k = lane + 32 * r;
-    rv[r] = k < nsets * nec ? gmom[k] : 0.f;
-  }
-#pragma unroll
-  for (int r = 0; r < RR; ++r) {
-    const int k = lane + 32 * r;
-    if (k < nsets * nec) raw[k] = rv[r];
-  }
-  __syncwarp();
+  // the stored moments are in shared memory (copied asynchronously at the start of the kernel)
+  const float* raw = gmom;
   // lane q builds entry q of every (set, width) table: its three component indices are fixed
   if (lane < MOM_Q) {
     const int u0 = c_mom_up[lane][0], u1 = c_mom_up[lane][1], u2 = c_mom_up[lane][2], dq = mom_deg(lane) + 1;
@@ -1029,7 +1025,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
 
 // ------------------------------------------------------------------------------------ force
 template <int NEK, int NZK, bool GEN>
-__global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
+__global__ void __launch_bounds__(128, 4) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
                                                     const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                                     const int* __restrict__ nb_cnt, const float* __restrict__ dEdG, int gstride,
@@ -1039,12 +1035,21 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
   const bool kx = GEN && P.kx;  // a compile-time false in the GAUSS-only instances
-  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, kx, gstride), cap, NEK, kx);
+  const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, kx, gstride + mstride), cap, NEK, kx);
+  float* gm = S.gi + gstride;  // the centre's stored moments
   const int I = clamp_type(type[i], P.ntypes);
-  // the centre's dE/dG row into shared memory: every block reads it several times
-  for (int k = lane; k < P.nin[I]; k += 32) S.gi[k] = dEdG[(size_t)i * gstride + k];
+  // the centre's dE/dG row (read by every block) and moment row into shared memory, in flight
+  // while the neighbours are staged (rows are 16-byte aligned: gstride and mstride are
+  // multiples of four floats)
+  for (int k = 4 * lane; k < P.nin[I]; k += 128) cp_async16(S.gi + k, dEdG + (size_t)i * gstride + k);
+  cp_async_commit();
+  if (mstride > 0)
+    for (int k = 4 * lane; k < mstride; k += 128) cp_async16(gm + k, mom + (size_t)i * mstride + k);
+  cp_async_commit();
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
   const bool cc = cutoff_cache(S, P, I, n);
+  cp_async_wait<1>();  // the dE/dG row
+  __syncwarp();
   const float* gi = S.gi;
 
   // ---- radial chain rule: W_p = BasisR::force(d) * u_p (basis_radial.cpp:371-380, nnp.cpp:441-446);
@@ -1087,6 +1092,9 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
   }
   __syncwarp();
 
+  cp_async_wait<0>();  // the moment row
+  __syncwarp();
+
   // ---- angular chain rule
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
@@ -1096,7 +1104,7 @@ __global__ void __launch_bounds__(128) force_kernel(const __grid_constant__ PotP
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
       if (A.mom) {
-        force_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, mom + (size_t)i * mstride + A.moff, gi);
+        force_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, gm + A.moff, gi);
         continue;
       }
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, false);
@@ -1313,7 +1321,7 @@ template <int NEK, int NZK, bool GEN>
 static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  force_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps, GEN && P.kx, B.gstride), st>>>(
+  force_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps, GEN && P.kx, B.gstride + P.mstride), st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
 }
 
