@@ -73,11 +73,13 @@ __global__ void __launch_bounds__(128) gather_kernel(int a0, int natoms, int cap
   warp_pair_sum(sx);
   warp_pair_sum(sy);
   warp_pair_sum(sz);
-  const double fx = sx.value(), fy = sy.value(), fz = sz.value();
-  if (lane == 0) {
-    force[3 * (size_t)j] = fx;
-    force[3 * (size_t)j + 1] = fy;
-    force[3 * (size_t)j + 2] = fz;
+  // lane k < 3 turns component k's pair into FP64: three FP64 instructions per atom, not nine
+  const float hy = __shfl_sync(0xffffffffu, sy.hi, 0), ly = __shfl_sync(0xffffffffu, sy.lo, 0);
+  const float hz = __shfl_sync(0xffffffffu, sz.hi, 0), lz = __shfl_sync(0xffffffffu, sz.lo, 0);
+  const float hx = __shfl_sync(0xffffffffu, sx.hi, 0), lx = __shfl_sync(0xffffffffu, sx.lo, 0);
+  if (lane < 3) {
+    const float h = lane == 0 ? hx : (lane == 1 ? hy : hz), l = lane == 0 ? lx : (lane == 1 ? ly : lz);
+    force[3 * (size_t)j + lane] = (double)h + (double)l;
   }
 }
 
