@@ -477,8 +477,10 @@ int launch_network_bf16(const BatchDev& B, const NetsP&, const void* tc, int nty
   const int need = TC_HMAX * (1 + (maxl - 2));
   uint32_t cols = 32;
   while ((int)cols < need) cols <<= 1;
-  // at least 120 KB of shared memory: one CTA per SM keeps TMEM demand within 512 columns
-  smem = std::max(smem, 120 * 1024);
+  // TMEM has 512 columns per SM and tcgen05.alloc waits while they are taken: the shared-memory
+  // request bounds the CTAs per SM so that their columns always fit.  Two CTAs when two
+  // allocations fit (80 KB: a third CTA does not fit in 228 KB), else one (120 KB).
+  smem = std::max(smem, (2 * cols <= 512) ? 80 * 1024 : 120 * 1024);
   static int attr_bytes = 0;
   if (smem > attr_bytes) {
     if (cudaFuncSetAttribute(network_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return -2;
