@@ -183,7 +183,7 @@ __device__ __forceinline__ float act_d(int act, float a) {
 __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constant__ TcNetsP N, int ntypes, const int* __restrict__ tc,
                                                             const int* __restrict__ perm, const float* __restrict__ G, int gstride,
                                                             float* __restrict__ eatom, float* __restrict__ dEdG, int want_grad,
-                                                            uint32_t tmem_cols, int* __restrict__ status) {
+                                                            uint32_t tmem_cols, int opk, int pcols, int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ uint64_t bar_w[2], bar_mma;
   __shared__ uint32_t tmem_slot;
@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
   const TcNetP& net = N.net[t];
   const int L = net.nlayer;
   const int ngemm = want_grad ? 2 * (L - 1) : (L - 1);
-  const int opbytes = TC_M * TC_HMAX * 2;
+  const int opbytes = TC_M * opk * 2;  // opk: the widest K of any GEMM of the batch's networks
   uint8_t* a_hi = smem_raw;                       // activation operand hi [128 x K]
   uint8_t* a_lo = smem_raw + opbytes;             // activation operand lo
   uint8_t* wbuf[2] = {smem_raw + 2 * opbytes, smem_raw + 2 * opbytes + ((net.maxblock + 1023) & ~1023)};
@@ -222,8 +222,8 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-  const uint32_t t_acc = tmem;               // accumulator columns [0, 128)
-  const uint32_t t_park = tmem + TC_HMAX;    // parked derivatives, 128 columns per hidden layer
+  const uint32_t t_acc = tmem;                      // accumulator columns [0, pcols)
+  const uint32_t t_park = tmem + (uint32_t)pcols;   // parked derivatives, pcols columns per hidden layer
 
   // weights of GEMM g -> buffer g&1 by one 1-D TMA bulk copy, completion on bar_w[g&1]
   auto load_w = [&](int g) {
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
         d[q] = act_d(net.act, a);
       }
       if (l < L - 2) {
-        tmem_st32(t_park + (uint32_t)(l * TC_HMAX) + lane_base + c0, d);
+        tmem_st32(t_park + (uint32_t)(l * pcols) + lane_base + c0, d);
         store_row_split(a_hi, a_lo, r, c0, n, v, 4);  // next layer's A operand
       } else {
         // last hidden layer: output node and the first back-propagated gradient
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
         tmem_ld32(t_acc + lane_base + c0, v);
         if (l > 0) {
           float d[32];
-          tmem_ld32(t_park + (uint32_t)((l - 1) * TC_HMAX) + lane_base + c0, d);
+          tmem_ld32(t_park + (uint32_t)((l - 1) * pcols) + lane_base + c0, d);
 #pragma unroll
           for (int q = 0; q < 32; ++q) v[q] *= d[q];
           store_row_split(a_hi, a_lo, r, c0, n, v, 4);
@@ -468,19 +468,25 @@ int launch_network_bf16(const BatchDev& B, const NetsP&, const void* tc, int nty
   if (!tc || !tcnets_host) return -1;
   if (B.natoms == 0) return 0;
   const TcNetsP& N = *reinterpret_cast<const TcNetsP*>(tcnets_host);
-  int smem = 0, maxl = 2;
+  // operand K stride and TMEM column block: the widest GEMM input / output of any network
+  int kmax = 16, maxl = 2, wblock = 0;
   for (int t = 0; t < ntypes; ++t) {
-    smem = std::max(smem, 2 * TC_M * TC_HMAX * 2 + 2 * ((N.net[t].maxblock + 1023) & ~1023));
-    maxl = std::max(maxl, N.net[t].nlayer);
+    const TcNetP& n = N.net[t];
+    for (int l = 0; l < n.nlayer; ++l) kmax = std::max(kmax, n.dims[l]);
+    maxl = std::max(maxl, n.nlayer);
+    wblock = std::max(wblock, (n.maxblock + 1023) & ~1023);
   }
-  // accumulator (128 columns) + one parked derivative block per hidden layer but the last
-  const int need = TC_HMAX * (1 + (maxl - 2));
+  const int opk = (kmax + 15) / 16 * 16;
+  const int pcols = (kmax + 31) / 32 * 32;
+  int smem = 2 * TC_M * opk * 2 + 2 * wblock;
+  // accumulator + one parked derivative block per hidden layer but the last
+  const int need = pcols * (1 + (maxl - 2));
   uint32_t cols = 32;
   while ((int)cols < need) cols <<= 1;
   // TMEM has 512 columns per SM and tcgen05.alloc waits while they are taken: the shared-memory
-  // request bounds the CTAs per SM so that their columns always fit.  Two CTAs when two
-  // allocations fit (80 KB: a third CTA does not fit in 228 KB), else one (120 KB).
-  smem = std::max(smem, (2 * cols <= 512) ? 80 * 1024 : 120 * 1024);
+  // request bounds the CTAs per SM (228 KB of shared memory) so that their columns always fit.
+  const int fit = 512 / (int)cols;
+  smem = std::max(smem, 228 * 1024 / (fit + 1) + 1024);
   static int attr_bytes = 0;
   if (smem > attr_bytes) {
     if (cudaFuncSetAttribute(network_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return -2;
@@ -488,7 +494,7 @@ int launch_network_bf16(const BatchDev& B, const NetsP&, const void* tc, int nty
   }
   const int tiles = (B.natoms + TC_M - 1) / TC_M + ntypes;
   network_tc_kernel<<<tiles, 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride, B.eatom, B.dEdG, want_grad, cols,
-                                             B.status);
+                                             opk, pcols, B.status);
   return 0;
 }
 
