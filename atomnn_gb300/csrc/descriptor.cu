@@ -1025,7 +1025,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
 
 // ------------------------------------------------------------------------------------ force
 template <int NEK, int NZK, bool GEN>
-__global__ void __launch_bounds__(128, 4) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
+__global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ PotParams P, int a0, int natoms, int cap,
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
                                                     const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                                     const int* __restrict__ nb_cnt, const float* __restrict__ dEdG, int gstride,

@@ -194,7 +194,7 @@ static int estimate_cap(const nnpgpu_ctx* c, int nstruc, const int* natoms, cons
     const double* R = cell + 9 * s;
     const double vol = std::fabs(R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]));
     double nb;
-    if (vol > 0) nb = natoms[s] / vol * 4.0 / 3.0 * M_PI * std::pow(rc + 0.5, 3) * 1.25 + 16;
+    if (vol > 0) nb = natoms[s] / vol * 4.0 / 3.0 * M_PI * std::pow(rc + 0.5, 3) * 1.1 + 16;
     else nb = natoms[s];
     best = std::max(best, nb);
   }
