@@ -17,7 +17,7 @@ constexpr int NIN_MAX = 256;                       // network inputs
 constexpr int MOM_N = 4;                           // largest zeta of a moment-tensor block
 constexpr int MOM_C = 35;                          // symmetric tensor components of degree 0..MOM_N
 constexpr int MOM_Q = 20;                          // components of degree 0..MOM_N-1
-constexpr int MOM_EX = 8 * MOM_Q + 2 * MOM_C + 2;  // per-width floats a moment block needs in shared memory
+constexpr int MOM_EX = 8 * MOM_Q;                  // per-width floats a moment block needs in shared memory
 constexpr int NLAYER_MAX = 4;                      // network layers (hidden + output)
 constexpr int HID_MAX = 256;                       // nodes per layer
 
@@ -116,6 +116,12 @@ struct StrucMeta {
   int pad4;
   float dmax2f, fro2f;   // FP32 copies of dMax2 and fro^2, and of the shifts, for the FP32 tests
   float shiftsf[18];
+  // image shells (mode 1): the images of lattice vectors sorted by decreasing norm (perm[a] is
+  // the column of sorted vector a) run over [-shell[a], shell[a]]; an image n can be within rc
+  // of a difference o only if |(R^-1 o)_c - n_c| <= hrc[c] = rc |row c of R^-1| + margin
+  float rinvf[9];        // R^-1 in FP32, column-major
+  float hrc[3];
+  int shell[3], perm[3];
 };
 // One lattice shift of the image box, in the reference's enumeration order (vf = v in FP32).
 struct ImgEntry {

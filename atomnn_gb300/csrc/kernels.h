@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
+
 #include "common.cuh"
 
 namespace nnpgpu {
@@ -73,6 +75,22 @@ int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps
 int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
 size_t symm_smem_bytes(int cap, int ne, int warps);
 size_t force_smem_bytes(int cap, int ne, int warps, bool kx, int gstride);
+// Image-shell box of a mode-1 structure (StrucMeta::rinvf/hrc/shell/perm): inv is R^-1 (rows),
+// shell and perm as enumerated for the image list.  Shared by the batched and no-allocation
+// set-ups.
+inline void set_image_box(StrucMeta& m, const double inv[3][3], double rc, const int shell[3], const int perm[3]) {
+  for (int k = 0; k < 9; ++k) m.rinvf[k] = (float)m.RInv[k];
+  for (int c = 0; c < 3; ++c) {
+    // |(R^-1 t)_c| <= |row c of R^-1| |t|; 2e-3 in fractional units covers the FP32 evaluation
+    // and the decision margin many times over
+    double h2 = 0.0;
+    for (int q = 0; q < 3; ++q) h2 += inv[c][q] * inv[c][q];
+    m.hrc[c] = (float)(rc * std::sqrt(h2) + 2e-3);
+    m.shell[c] = shell[c];
+    m.perm[c] = perm[c];
+  }
+}
+
 // atomic networks: FP32 SIMT path and BF16 tensor-core path
 void launch_type_sort(const BatchDev& B, int ntypes, cudaStream_t st);
 size_t type_sort_ints(int natoms);  // ints of the type_count buffer for a batch of natoms

@@ -490,23 +490,39 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       int D[3] = {0, 0, 0};
       int cnt = 0, best = -1;
       bool exact = false;  // FP64 replay for this pair
+      // the images that can lie within rc of the difference: a box in the sorted lattice
+      // coordinates, visited in the reference's order (image n = ((a+s0)(2s1+1) + b+s1)(2s2+1) + c+s2)
+      int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
       if (jl < nj) {
         bool ok = cell_diff_f32(S, si, fi, sfrac[j], sfloor[j], o0, o1, o2, D);
         if (ok) {
-          float mn = 3.4e38f, second = 3.4e38f;
-          for (int n = 0; n < nimg; ++n) {
-            const float t0 = o0 - im[n].vf[0], t1 = o1 - im[n].vf[1], t2 = o2 - im[n].vf[2];
-            const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
-            if (fabsf(d2 - rc2f) <= m) { ok = false; break; }
-            const bool keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
-            if (keep) {
-              ++cnt;
-              if (j != i) {
-                if (d2 < mn) { second = mn; mn = d2; best = n; }
-                else if (d2 < second) second = d2;
-              }
-            }
+          const float fr[3] = {S.rinvf[0] * o0 + S.rinvf[3] * o1 + S.rinvf[6] * o2, S.rinvf[1] * o0 + S.rinvf[4] * o1 + S.rinvf[7] * o2,
+                               S.rinvf[2] * o0 + S.rinvf[5] * o1 + S.rinvf[8] * o2};
+#pragma unroll
+          for (int a = 0; a < 3; ++a) {
+            const int col = S.perm[a];
+            const float f = col == 0 ? fr[0] : (col == 1 ? fr[1] : fr[2]);
+            const float h = col == 0 ? S.hrc[0] : (col == 1 ? S.hrc[1] : S.hrc[2]);
+            lo[a] = max(-S.shell[a], (int)ceilf(f - h));
+            hi[a] = min(S.shell[a], (int)floorf(f + h));
           }
+          float mn = 3.4e38f, second = 3.4e38f;
+          for (int a0 = lo[0]; a0 <= hi[0] && ok; ++a0)
+            for (int a1 = lo[1]; a1 <= hi[1] && ok; ++a1)
+              for (int a2 = lo[2]; a2 <= hi[2]; ++a2) {
+                const int n = ((a0 + S.shell[0]) * (2 * S.shell[1] + 1) + (a1 + S.shell[1])) * (2 * S.shell[2] + 1) + (a2 + S.shell[2]);
+                const float t0 = o0 - im[n].vf[0], t1 = o1 - im[n].vf[1], t2 = o2 - im[n].vf[2];
+                const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
+                if (fabsf(d2 - rc2f) <= m) { ok = false; break; }
+                const bool keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
+                if (keep) {
+                  ++cnt;
+                  if (j != i) {
+                    if (d2 < mn) { second = mn; mn = d2; best = n; }
+                    else if (d2 < second) second = d2;
+                  }
+                }
+              }
           // a near tie between the two closest kept images could flip the minimum-image flag;
           // with fewer than two kept images (or for the self pair) there is no tie to resolve
           if (ok && best >= 0 && second < 3.0e38f && second - mn <= m) ok = false;
@@ -542,27 +558,35 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       }
       int slot = count + incl - cnt;
       if (cnt > 0) {
-        for (int n = 0; n < nimg; ++n) {
-          float t0, t1, t2, dr;
-          bool keep;
-          if (exact) {
-            const double e0 = dsub(p0, im[n].v[0]), e1 = dsub(p1, im[n].v[1]), e2 = dsub(p2, im[n].v[2]);
-            const double d2 = sqn3(e0, e1, e2);
-            keep = (j != i) ? (d2 <= rc2) : (1e-6 < d2 && d2 <= rc2);
-            t0 = (float)e0; t1 = (float)e1; t2 = (float)e2;
-            dr = keep ? (float)sqrt(d2) : 0.f;
-          } else {
-            t0 = o0 - im[n].vf[0]; t1 = o1 - im[n].vf[1]; t2 = o2 - im[n].vf[2];
-            const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
-            keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
-            dr = sqrtf(d2);
-          }
-          if (keep) {
-            emit(slot, cap, j, t0, t1, t2, dr, pack_code(D[0] + im[n].n[0], D[1] + im[n].n[1], D[2] + im[n].n[2], n == best), oj, orr, oc,
-                 ot, sfrac);
-            ++slot;
-          }
+        // the exact replay visits every image, the FP32 path its box
+        if (exact) {
+          lo[0] = -S.shell[0]; lo[1] = -S.shell[1]; lo[2] = -S.shell[2];
+          hi[0] = S.shell[0]; hi[1] = S.shell[1]; hi[2] = S.shell[2];
         }
+        for (int a0 = lo[0]; a0 <= hi[0]; ++a0)
+          for (int a1 = lo[1]; a1 <= hi[1]; ++a1)
+            for (int a2 = lo[2]; a2 <= hi[2]; ++a2) {
+              const int n = ((a0 + S.shell[0]) * (2 * S.shell[1] + 1) + (a1 + S.shell[1])) * (2 * S.shell[2] + 1) + (a2 + S.shell[2]);
+              float t0, t1, t2, dr;
+              bool keep;
+              if (exact) {
+                const double e0 = dsub(p0, im[n].v[0]), e1 = dsub(p1, im[n].v[1]), e2 = dsub(p2, im[n].v[2]);
+                const double d2 = sqn3(e0, e1, e2);
+                keep = (j != i) ? (d2 <= rc2) : (1e-6 < d2 && d2 <= rc2);
+                t0 = (float)e0; t1 = (float)e1; t2 = (float)e2;
+                dr = keep ? (float)sqrt(d2) : 0.f;
+              } else {
+                t0 = o0 - im[n].vf[0]; t1 = o1 - im[n].vf[1]; t2 = o2 - im[n].vf[2];
+                const float d2 = t0 * t0 + t1 * t1 + t2 * t2;
+                keep = (j != i) ? (d2 <= rc2f) : (1e-6f < d2 && d2 <= rc2f);
+                dr = sqrtf(d2);
+              }
+              if (keep) {
+                emit(slot, cap, j, t0, t1, t2, dr, pack_code(D[0] + im[n].n[0], D[1] + im[n].n[1], D[2] + im[n].n[2], n == best), oj, orr, oc,
+                     ot, sfrac);
+                ++slot;
+              }
+            }
       }
       count += __shfl_sync(0xffffffffu, incl, 31);
     }

@@ -168,6 +168,7 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
     return;
   }
   m.mode = 1;
+  set_image_box(m, inv, rc, shell, perm);
   m.img0 = (int)imgs.size();
   for (int i = -shell[0]; i <= shell[0]; ++i)
     for (int j = -shell[1]; j <= shell[1]; ++j)

@@ -149,6 +149,7 @@ int fixed_meta(const double* cell, int natoms, double rc, StrucMeta& m, ImgEntry
   const long long want = (long long)(2 * shell[0] + 1) * (2 * shell[1] + 1) * (2 * shell[2] + 1);
   if (want > NOALLOC_MAX_IMAGES) return -2;
   m.mode = 1;
+  set_image_box(m, inv, rc, shell, perm);
   for (int i = -shell[0]; i <= shell[0]; ++i)
     for (int j = -shell[1]; j <= shell[1]; ++j)
       for (int k = -shell[2]; k <= shell[2]; ++k) {
