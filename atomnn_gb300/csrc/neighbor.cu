@@ -627,10 +627,13 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
 // (i,s).  Lists are sorted by neighbour index, so each lane binary-searches its own target.
 // A source without a partner (possible only for pairs within rounding of the cutoff, or ties
 // between equidistant images) is recorded as an orphan and added by a serial fix-up pass.
+// The minimum-image slots of a pair point at each other (each list holds one minimum-image
+// entry per neighbour), so pass 0 searches only from the lower index (i < j) and on a match sets
+// both entries; pass 1 visits the slots with i > j and searches only where pass 0 left no entry.
 __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int cap, const int* __restrict__ nb_j,
                                                       const int* __restrict__ nb_code, const int* __restrict__ nb_cnt,
                                                       int* __restrict__ nb_rev, int* __restrict__ orphans, int orphan_cap,
-                                                      int* __restrict__ status) {
+                                                      int* __restrict__ status, int pass) {
   const int lane = threadIdx.x & 31;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
@@ -639,6 +642,7 @@ __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int ca
     const size_t src = (size_t)i * cap + s;
     if (!code_min(nb_code[src])) continue;
     const int j = nb_j[src];
+    if (pass == 0 ? (i > j) : (i < j || nb_rev[src] >= 0)) continue;
     const int nj = min(nb_cnt[j], cap);
     const int* L = nb_j + (size_t)j * cap;
     int lo = 0, hi = nj;
@@ -652,6 +656,7 @@ __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int ca
       if (code_min(nb_code[(size_t)j * cap + t])) { found = t; break; }
     if (found >= 0) {
       nb_rev[(size_t)j * cap + found] = (int)src;
+      if (pass == 0) nb_rev[src] = (int)((size_t)j * cap + found);
     } else {
       const int k = atomicAdd(&status[ST_ORPHANS], 1);
       if (k < orphan_cap) orphans[k] = (int)src;
@@ -682,8 +687,9 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
 void launch_reverse(const BatchDev& B, cudaStream_t st) {
   if (B.natoms == 0) return;
   cudaMemsetAsync(B.nb_rev + (size_t)B.a0 * B.cap, 0xff, sizeof(int) * (size_t)B.natoms * B.cap, st);
-  reverse_kernel<<<(B.natoms + 3) / 4, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.nb_j, B.nb_code, B.nb_cnt, B.nb_rev, B.orphans,
-                                                     B.orphan_cap, B.status);
+  for (int pass = 0; pass < 2; ++pass)
+    reverse_kernel<<<(B.natoms + 3) / 4, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.nb_j, B.nb_code, B.nb_cnt, B.nb_rev, B.orphans,
+                                                       B.orphan_cap, B.status, pass);
 }
 
 }  // namespace nnpgpu

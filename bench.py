@@ -30,7 +30,7 @@ from atomnn_gb300 import workloads as W  # noqa: E402
 
 METRIC = "atoms/sec E+F (BF16 batched vs plain), p50/p99 latency, at force err ≤1e-3 eV/Å"
 WORKLOAD = "mixed512"
-KERNELS_PER_BATCH = 14  # frac, cell scan, cell fill, neighbor, reverse, symm, 3x type sort, network, force, gather, orphan, energy
+KERNELS_PER_BATCH = 15  # frac, cell scan, cell fill, neighbor, 2x reverse, symm, 3x type sort, network, force, gather, orphan, energy
 WORK_DIR = os.path.join(REPO, "atomnn_gb300", "_build", "workloads")
 
 
