@@ -243,7 +243,7 @@ def test_full_size_properties(engines):
         assert np.abs(Fs[0][r * 1728:(r + 1) * 1728] - Fc[0]).max() < F_TOL
 
 
-# ---- BF16 tensor-core networks: the spec gate is force RMSE <= 1e-3 eV/A against the
+# ---- BF16 tensor-core networks: the accuracy gate is force RMSE <= 1e-3 eV/A against the
 # FP64 oracle; the energy per atom is held to 1e-3 eV/atom.
 BF16_F_RMSE = 1e-3
 BF16_E_TOL = 1e-3
