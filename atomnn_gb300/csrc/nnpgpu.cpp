@@ -948,6 +948,80 @@ extern "C" int nnpgpu_nparams(const nnpgpu_ctx* c, int type) {
 // The energy trainer's batch error and gradient (NNPTE::error, src/nnp/nnpte.cpp:870-921): one
 // batched energy pass (FP32 networks, energies without the vacuum energies), then the loss and the
 // parameter gradient on the device (network.cu).
+extern "C" int nnpgpu_get_params(const nnpgpu_ctx* c, int type, double* p) {
+  if (!c || type < 0 || type >= c->pot.ntypes || !p) return NNPGPU_ERR_INVALID;
+  const HNet& n = c->pot.nets[type];
+  size_t k = 0;
+  for (size_t l = 0; l < n.nodes.size(); ++l)
+    for (int r = 0; r < n.nodes[l]; ++r) p[k++] = n.b[l][r];
+  for (size_t l = 0; l < n.nodes.size(); ++l) {
+    const int C = l == 0 ? n.nin : n.nodes[l - 1];
+    for (int m = 0; m < C; ++m)
+      for (int r = 0; r < n.nodes[l]; ++r) p[k++] = n.w[l][(size_t)r * C + m];
+  }
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_set_params(nnpgpu_ctx* c, int type, const double* p) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (type < 0 || type >= c->pot.ntypes || !p) return set_error(c, NNPGPU_ERR_INVALID, "set_params: invalid type or parameters");
+  if (c->serving) return set_error(c, NNPGPU_ERR_BUSY, "set_params: stop serving first");
+  HNet& n = c->pot.nets[type];
+  const int np = net_param_count(c, type);
+  for (int k = 0; k < np; ++k)
+    if (!std::isfinite(p[k])) return set_error(c, NNPGPU_ERR_INVALID, "set_params: non-finite parameter");
+  size_t k = 0;
+  for (size_t l = 0; l < n.nodes.size(); ++l)
+    for (int r = 0; r < n.nodes[l]; ++r) n.b[l][r] = p[k++];
+  for (size_t l = 0; l < n.nodes.size(); ++l) {
+    const int C = l == 0 ? n.nin : n.nodes[l - 1];
+    for (int m = 0; m < C; ++m)
+      for (int r = 0; r < n.nodes[l]; ++r) n.w[l][(size_t)r * C + m] = p[k++];
+  }
+  if (!c->netbuf) return NNPGPU_OK;  // no device: the host copy is all there is
+  // device copies: FP32 weights in place, the tensor-core blob packed anew; captured graphs hold
+  // the output bias and the blob pointer by value, so they are rebuilt on the next calls
+  cudaSetDevice(c->device);
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  const NetP& q = c->nets.net[type];
+  for (size_t l = 0; l < n.nodes.size() && e == cudaSuccess; ++l) {
+    const int R = n.nodes[l], C = l == 0 ? n.nin : n.nodes[l - 1];
+    std::vector<float> w((size_t)R * C), wt((size_t)R * C), b(R);
+    for (int r = 0; r < R; ++r) {
+      b[r] = (float)n.b[l][r];
+      for (int m = 0; m < C; ++m) {
+        w[(size_t)r * C + m] = (float)n.w[l][(size_t)r * C + m];
+        wt[(size_t)m * R + r] = (float)n.w[l][(size_t)r * C + m];
+      }
+    }
+    e = cudaMemcpy((void*)q.w[l], w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy((void*)q.wt[l], wt.data(), sizeof(float) * wt.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy((void*)q.b[l], b.data(), sizeof(float) * b.size(), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "set_params");
+  drop_graphs(c);
+  c->shapes_seen.clear();
+  if (c->tcbuf) {
+    cudaFree(c->tcbuf);
+    c->used -= c->tcbytes;
+    c->tcbuf = nullptr;
+    c->tcbytes = 0;
+  }
+  prepare_tc_weights(c);  // leaves the tensor-core path off if the networks do not fit it, as at creation
+  return NNPGPU_OK;
+}
+
+extern "C" int nnpgpu_write_potential(nnpgpu_ctx* c, const char* path) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (!path) return set_error(c, NNPGPU_ERR_INVALID, "write_potential: no file");
+  try {
+    write_potential(c->pot, path);
+  } catch (PotError& e) {
+    return set_error(c, e.code, e.what());
+  }
+  return NNPGPU_OK;
+}
+
 extern "C" int nnpgpu_train_grad(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
                                  const double* energy_ref, int loss, double delta, double* error, double* grad) {
   if (!c) return NNPGPU_ERR_INVALID;

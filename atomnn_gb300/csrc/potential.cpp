@@ -80,11 +80,11 @@ HPot read_potential(const char* path) {
         for (auto& c : tag) c = (char)std::toupper((unsigned char)c);
         const bool has = k + 1 < tt.size();
         if (tag == "NAME" && has) P.types[n].name = tt[++k];
-        else if (tag == "MASS" && has) P.types[n].mass = std::atof(tt[++k].c_str());
-        else if (tag == "ENERGY" && has) P.types[n].energy = std::atof(tt[++k].c_str());
+        else if (tag == "MASS" && has) { P.types[n].mass = std::atof(tt[++k].c_str()); P.types[n].has_mass = true; }
+        else if (tag == "ENERGY" && has) { P.types[n].energy = std::atof(tt[++k].c_str()); P.types[n].has_energy = true; }
         else if (has && (tag == "CHARGE" || tag == "CHI" || tag == "ETA" || tag == "JS" || tag == "C6" || tag == "RVDW" ||
                          tag == "RCOV"))
-          ++k;
+          P.types[n].other[tag] = std::atof(tt[++k].c_str());
       }
       P.index[P.types[n].name] = n;
     }
@@ -173,6 +173,7 @@ HPot read_potential(const char* path) {
       for (int x : nodes)
         if (x <= 0) throw PotError(NNPGPU_ERR_IO, "potential file: invalid layer size");
       const std::string neuron = tok(L.next(), 1, L);
+      net.neuron = neuron;
       net.act = neuron == "TANH" ? ACT_TANH : neuron == "LINEAR" ? ACT_LINEAR : neuron == "SIGMOID" ? ACT_SIGMOID : -1;
       if (net.act < 0) {
         static const char* known[] = {"ISRU", "ARCTAN", "SOFTSIGN", "RELU", "SOFTPLUS", "ELU", "GELU", "SWISH", "MISH",
@@ -362,6 +363,72 @@ std::vector<float> build_ang_tables(const HPot& pot, PotParams& P) {
       }
     }
   return tab;
+}
+
+void write_potential(const HPot& P, const char* path) {
+  FILE* f = std::fopen(path, "w");
+  if (!f) throw PotError(NNPGPU_ERR_IO, std::string("could not open \"") + path + "\" for writing");
+  static const char* cut_names[] = {"UNKNOWN", "STEP", "COS", "TANH"};
+  static const char* norm_names[] = {"UNKNOWN", "UNIT", "VOL"};
+  static const char* rad_names[] = {"UNKNOWN", "GAUSSIAN", "TANH", "SOFTPLUS", "LOGCOSH", "SWISH", "MISH"};
+  static const char* ang_names[] = {"UNKNOWN", "GAUSS", "IPOWP", "IPOWS", "SECHP", "SECHS"};
+  auto name = [](const char* const* names, int n, int v) { return (v >= 0 && v < n) ? names[v] : names[0]; };
+  std::fprintf(f, "ann\n");
+  std::fprintf(f, "ntypes %i\n", P.ntypes);
+  for (const HType& t : P.types) {  // Type::write (src/nnp/type.cpp:125-138): flagged properties in this order
+    std::fprintf(f, "name %s ", t.name.c_str());
+    if (t.has_mass) std::fprintf(f, "mass %f ", t.mass);
+    if (t.has_energy) std::fprintf(f, "energy %f ", t.energy);
+    for (const char* key : {"CHARGE", "CHI", "ETA", "JS", "C6", "RVDW", "RCOV"}) {
+      auto it = t.other.find(key);
+      if (it == t.other.end()) continue;
+      std::string low(key);
+      for (char& ch : low) ch = (char)std::tolower((unsigned char)ch);
+      std::fprintf(f, "%s %f ", low.c_str(), it->second);
+    }
+    std::fprintf(f, "\n");
+  }
+  std::fprintf(f, "rc %f\n", P.rc);
+  for (int i = 0; i < P.ntypes; ++i) {
+    std::fprintf(f, "basis %s\n", P.types[i].name.c_str());
+    for (int j = 0; j < P.ntypes; ++j) {  // BasisR::write (src/nnp/basis_radial.cpp:107-116)
+      const HBasisR& b = P.rad[i][j];
+      std::fprintf(f, "basis_radial %s\n", P.types[j].name.c_str());
+      std::fprintf(f, "BasisR %s %s %f %s %i\n", name(norm_names, 3, b.norm), name(cut_names, 4, b.cut), b.rc, name(rad_names, 7, b.phi),
+                   (int)b.rs.size());
+      for (size_t k = 0; k < b.rs.size(); ++k) std::fprintf(f, "\t%f %f\n", b.rs[k], b.eta[k]);
+    }
+    for (int j = 0; j < P.ntypes; ++j)
+      for (int k = j; k < P.ntypes; ++k) {  // BasisA::write (src/nnp/basis_angular.cpp:97-106)
+        const HBasisA& b = P.ang[i][lidx(j, k)];
+        std::fprintf(f, "basis_angular %s %s\n", P.types[j].name.c_str(), P.types[k].name.c_str());
+        std::fprintf(f, "BasisA %s %s %f %s %i %i\n", name(norm_names, 3, b.norm), name(cut_names, 4, b.cut), b.rc, name(ang_names, 6, b.phi),
+                     (int)b.eta.size(), b.alpha);
+        for (size_t q = 0; q < b.eta.size(); ++q) std::fprintf(f, "\t%f %f %i\n", b.eta[q], b.zeta[q], b.lam[q]);
+      }
+  }
+  for (int n = 0; n < P.ntypes; ++n) {  // ANN::write (src/ml/nn.cpp:1284-1323)
+    const HNet& net = P.nets[n];
+    std::fprintf(f, "nn %s\n", P.types[n].name.c_str());
+    std::fprintf(f, "nn %i ", net.nin);
+    for (int x : net.nodes) std::fprintf(f, "%i ", x);
+    std::fprintf(f, "\n");
+    std::fprintf(f, "neuron %s\n", net.neuron.c_str());
+    auto row = [&](const char* tag, const std::vector<double>& v) {
+      std::fprintf(f, "%s ", tag);
+      for (double x : v) std::fprintf(f, "%.15f ", x);
+      std::fprintf(f, "\n");
+    };
+    row("inpw", net.inpw);
+    row("outw", net.outw);
+    row("inpb", net.inpb);
+    row("outb", net.outb);
+    for (size_t l = 0; l < net.b.size(); ++l) row(("bias[" + std::to_string(l + 1) + "]").c_str(), net.b[l]);
+    for (size_t l = 0; l < net.w.size(); ++l)
+      row(("weight[" + std::to_string(l) + "," + std::to_string(l + 1) + "]").c_str(), net.w[l]);
+  }
+  const bool ok = std::ferror(f) == 0;
+  if (std::fclose(f) != 0 || !ok) throw PotError(NNPGPU_ERR_IO, std::string("write error on \"") + path + "\"");
 }
 
 }  // namespace nnpgpu

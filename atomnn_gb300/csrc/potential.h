@@ -22,13 +22,16 @@ struct HBasisA {  // BasisA (src/nnp/basis_angular.hpp:53-115)
 };
 struct HNet {  // NN::ANN (src/ml/nn.hpp:218-341)
   int nin = 0, act = 0;
+  std::string neuron;  // as written in the file
   std::vector<int> nodes;
   std::vector<double> inpw, inpb, outw, outb;
   std::vector<std::vector<double>> b, w;  // w[l] row-major [nodes[l]][cols]
 };
-struct HType {  // Type (src/nnp/type.hpp:22-94): name, mass, vacuum energy
+struct HType {  // Type (src/nnp/type.hpp:22-94): name, mass, vacuum energy, other properties
   std::string name;
   double mass = 0, energy = 0;
+  bool has_mass = false, has_energy = false;
+  std::map<std::string, double> other;  // CHARGE, CHI, ETA, JS, C6, RVDW, RCOV when given
 };
 struct HPot {  // NNP (src/nnp/nnp.hpp:68-121)
   double rc = 0;
@@ -49,6 +52,9 @@ struct PotError : std::runtime_error {
 
 // Parses the text format written by NNP::write (src/nnp/nnp.cpp:198-237); throws PotError.
 HPot read_potential(const char* path);
+// Writes it (NNP::write with Type::write, BasisR::write, BasisA::write and ANN::write: same
+// tokens, order and number formats); throws PotError(NNPGPU_ERR_IO).
+void write_potential(const HPot& pot, const char* path);
 // Fills the kernel tables; throws PotError(NNPGPU_ERR_UNSUPPORTED) for forms the kernels lack.
 void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max);
 // the per-block angular tables (AngP::tab) after build_tables: sets each block's tab offset and

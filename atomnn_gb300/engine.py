@@ -20,7 +20,7 @@ EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntype
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
            "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
            "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad", "nnpgpu_energy_symm",
-           "nnpgpu_train_force_grad"]
+           "nnpgpu_train_force_grad", "nnpgpu_get_params", "nnpgpu_set_params", "nnpgpu_write_potential"]
 
 _lib = None
 
@@ -75,6 +75,9 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_train_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, ip, dp, vp, vp]
     L.nnpgpu_energy_symm.argtypes = [vp, ip, vp, vp, vp, ip, ip, vp]
     L.nnpgpu_train_force_grad.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp, dp, ip, dp, vp, vp]
+    L.nnpgpu_get_params.argtypes = [vp, ip, vp]
+    L.nnpgpu_set_params.argtypes = [vp, ip, vp]
+    L.nnpgpu_write_potential.argtypes = [vp, cp]
     L.nnpgpu_md_destroy.argtypes = [vp]
     L.nnpgpu_md_destroy.restype = None
     L.nnpgpu_serve_start.argtypes = [vp, ctypes.POINTER(ServeOpts)]
@@ -224,6 +227,23 @@ class Engine:
         self._check(self.lib.nnpgpu_train_force_grad(self._ctx, len(structures), _p(natoms), _p(posn), _p(species), _p(cell), _p(eref),
                                                      _p(fref), float(beta), self.LOSS[loss], float(delta), _p(err), _p(grad)))
         return err[0], err[1], err[2], grad
+
+    def params(self, t):
+        """Network parameters of species t (nnpgpu_get_params; biases, then weights input-outer)."""
+        p = np.zeros(self.nparams(t))
+        self._check(self.lib.nnpgpu_get_params(self._ctx, t, _p(p)))
+        return p
+
+    def set_params(self, t, p):
+        """Replace the network parameters of species t (nnpgpu_set_params)."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        if p.size != self.nparams(t):
+            raise ValueError("species %d has %d parameters" % (t, self.nparams(t)))
+        self._check(self.lib.nnpgpu_set_params(self._ctx, t, _p(p)))
+
+    def write_potential(self, path):
+        """The potential with its current parameters in the reference's text format."""
+        self._check(self.lib.nnpgpu_write_potential(self._ctx, path.encode()))
 
     def energy_symm(self, natoms, species, symm, flags=0):
         """Energies of structures from stored descriptors (nnpgpu_energy_symm): natoms per

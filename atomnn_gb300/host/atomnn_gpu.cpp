@@ -314,6 +314,12 @@ void NNP::read(const char* file, NNP& nnp, const nnpgpu_opts* opts) {
   g_last = holder;
 }
 
+void NNP::write(const char* file, const NNP& nnp) {
+  if (!nnp.ctx_) throw std::runtime_error("NNP::write: no potential read");
+  if (!file) throw std::invalid_argument("NNP::write: no file");
+  check(nnp.ctx(), nnpgpu_write_potential(nnp.ctx(), file), "NNP::write");
+}
+
 void NNP::init(const NNP& nnp, Structure& struc) {
   for (int i = 0; i < struc.nAtoms(); ++i) {
     const int t = struc.type(i);

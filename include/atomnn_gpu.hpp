@@ -226,6 +226,9 @@ class NNP {
 
   // NNP::read(const char*, NNP&) (src/nnp/nnp.cpp:182-191,244-308); opts may be null
   static void read(const char* file, NNP& nnp, const nnpgpu_opts* opts = nullptr);
+  // NNP::write(const char*, const NNP&) (src/nnp/nnp.cpp:198-237): the potential with the
+  // networks' current parameters (as set through nnpgpu_set_params by a trainer)
+  static void write(const char* file, const NNP& nnp);
   // NNP::init: sizes struc.symm(i) to the input size of atom i's type
   static void init(const NNP& nnp, Structure& struc);
   // NNP::symm: struc.symm(i) for every atom (nnp.cpp:334-381)

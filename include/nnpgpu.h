@@ -141,6 +141,14 @@ int nnpgpu_energy_symm(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const int
  *   layer's weights with the input index outer and the node index inner).
  * Descriptors are computed from the positions on each call (FP32, FP32 networks). */
 int nnpgpu_nparams(const nnpgpu_ctx* ctx, int type);
+/* the networks' parameters in the same order, to read and to replace (a trainer's update; later
+ * evaluations use them; refused with NNPGPU_ERR_BUSY while serving), and the potential with its
+ * current parameters written in the reference's text format (NNP::write, src/nnp/nnp.cpp:198-237).
+ * Without a device (nnpgpu_create returned NNPGPU_ERR_CUDA but a context) they act on the parsed
+ * potential alone. */
+int nnpgpu_get_params(const nnpgpu_ctx* ctx, int type, double* params);
+int nnpgpu_set_params(nnpgpu_ctx* ctx, int type, const double* params);
+int nnpgpu_write_potential(nnpgpu_ctx* ctx, const char* path);
 /* ---- training with forces: the force trainer's loss (NNPTEF::error, src/nnp/nnptef.cpp:1043-1135)
  *   sum_s loss(dE_s) + sum over atoms 0.5 beta |(F - F_ref)/N_s|^2,
  * F the forces of NNP::force (minimum-image rule), E without vacuum energies, loss and delta as

@@ -95,3 +95,60 @@ def test_tune_shapes_validated(native_lib):
         assert native_lib.nnpgpu_autotune(ctx, 0, None, None, None, None, 0, None, 0) == engine.ERR_INVALID
     finally:
         native_lib.nnpgpu_destroy(ctx)
+
+
+def _ctx_without_device(lib, path):
+    """A context whose potential is parsed; on a machine without a GPU nnpgpu_create returns
+    NNPGPU_ERR_CUDA together with it."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: covered by tests/test_gpu_train.py")
+    from atomnn_gb300 import engine
+    ctx = ctypes.c_void_p()
+    rc = lib.nnpgpu_create(path.encode(), None, ctypes.byref(ctx))
+    assert rc == engine.ERR_CUDA and ctx
+    return ctx
+
+
+def test_write_potential_reproduces_the_file(native_lib, tmp_path):
+    """nnpgpu_write_potential writes NNP::write's format: the file the workload writer made (the
+    same tokens and number formats) comes back byte for byte."""
+    from atomnn_gb300 import engine
+    src = os.path.join(GOLDEN, "mixed512.nnp")
+    ctx = _ctx_without_device(native_lib, src)
+    try:
+        out = tmp_path / "copy.nnp"
+        assert native_lib.nnpgpu_write_potential(ctx, str(out).encode()) == engine.OK
+        assert out.read_bytes() == open(src, "rb").read()
+        assert native_lib.nnpgpu_write_potential(ctx, str(tmp_path / "no" / "dir.nnp").encode()) == engine.ERR_IO
+    finally:
+        native_lib.nnpgpu_destroy(ctx)
+
+
+def test_params_roundtrip_through_the_potential_file(native_lib, oracle_lib, tmp_path):
+    """get_params gives the oracle's parameters in the reference's order; set_params followed by
+    write_potential gives a file whose networks carry the new values (to the 15 decimals of
+    ANN::write)."""
+    import numpy as np
+    from atomnn_gb300 import engine
+    src = os.path.join(GOLDEN, "mixed512.nnp")
+    orc = oracle_lib.OracleNNP(src)
+    ctx = _ctx_without_device(native_lib, src)
+    try:
+        for t in range(orc.ntypes):
+            n = native_lib.nnpgpu_nparams(ctx, t)
+            p = np.zeros(n)
+            assert native_lib.nnpgpu_get_params(ctx, t, p.ctypes.data_as(ctypes.c_void_p)) == engine.OK
+            np.testing.assert_array_equal(p, orc.params(t))
+            q = p + np.random.default_rng(t).normal(0.0, 0.01, n)
+            assert native_lib.nnpgpu_set_params(ctx, t, q.ctypes.data_as(ctypes.c_void_p)) == engine.OK
+        bad = np.full(native_lib.nnpgpu_nparams(ctx, 0), np.nan)
+        assert native_lib.nnpgpu_set_params(ctx, 0, bad.ctypes.data_as(ctypes.c_void_p)) == engine.ERR_INVALID
+        out = str(tmp_path / "new.nnp")
+        assert native_lib.nnpgpu_write_potential(ctx, out.encode()) == engine.OK
+        orc2 = oracle_lib.OracleNNP(out)
+        for t in range(orc.ntypes):
+            q = orc.params(t) + np.random.default_rng(t).normal(0.0, 0.01, len(orc.params(t)))
+            np.testing.assert_allclose(orc2.params(t), q, rtol=0, atol=1e-14)
+    finally:
+        native_lib.nnpgpu_destroy(ctx)

@@ -106,3 +106,32 @@ def test_train_force_grad_rejects_bad_input(pair):
         eng.train_force_grad(strucs, eref, fref, -1.0, "MSE")
     with pytest.raises(engine.NNPGPUError):
         eng.train_force_grad(strucs, eref, fref, 1.0, "ASINH", delta=0.0)
+
+
+def test_set_params_updates_the_device_networks(native_lib, oracle_lib, tmp_path):
+    """A trainer's update through nnpgpu_set_params reaches the FP32 and tensor-core networks
+    (including launch sequences captured before it): energies and forces equal the oracle's on
+    the potential that nnpgpu_write_potential writes afterwards."""
+    from atomnn_gb300 import engine
+    eng = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"))
+    try:
+        strucs = W.make_structures("mixed512", seed=91, count=3, sizes=[40, 300, 900])
+        for flags in (engine.BF16, 0):
+            for _ in range(3):  # the batch shape's launch sequence is captured
+                eng.compute(strucs, engine.ENERGY | engine.FORCE | engine.BATCHED | flags)
+        rng = np.random.default_rng(7)
+        for t in range(eng.ntypes):
+            eng.set_params(t, eng.params(t) * (1.0 + 0.05 * rng.normal(size=eng.nparams(t))))
+        path = str(tmp_path / "updated.nnp")
+        eng.write_potential(path)
+        orc = oracle_lib.OracleNNP(path)
+        e, F, _ = eng.compute(strucs, engine.ENERGY | engine.FORCE | engine.BATCHED)
+        eb, Fb, _ = eng.compute(strucs, engine.ENERGY | engine.FORCE | engine.BATCHED | engine.BF16)
+        for k, s in enumerate(strucs):
+            eo, Fo, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+            assert abs(e[k] - eo) / s.natoms <= 1e-5
+            assert np.abs(F[k] - Fo).max() <= 1e-4 * max(1.0, np.abs(Fo).max() / 2.0)
+            assert abs(eb[k] - eo) / s.natoms <= 1e-3
+            assert np.sqrt(((Fb[k] - Fo) ** 2).mean()) <= 1e-3
+    finally:
+        eng.close()
