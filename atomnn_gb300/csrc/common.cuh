@@ -133,7 +133,7 @@ struct ImgEntry {
 
 // Device status words (one int array per context).
 enum { ST_MAXCOUNT = 0, ST_ORPHANS = 1, ST_ERROR = 2, ST_DEBUG = 8, ST_WORDS = 32 };
-enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_ORPHANS = 4, ERR_TIMEOUT = 8 };
+enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_ORPHANS = 4, ERR_TIMEOUT = 8, ERR_DRAIN = 16 };
 
 #ifdef __CUDACC__
 // ---- exact FP64 helpers: fixed evaluation order and no FMA contraction, so that the GPU

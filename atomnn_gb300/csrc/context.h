@@ -78,6 +78,7 @@ struct nnpgpu_ctx {
   size_t budget = 0, used = 0;
   int cap_hint = 0;
   nnpgpu::TuneCfg tune;
+  int tc_wait_limit = 1 << 22;  // polls of each mbarrier wait of the tensor-core networks (nnpgpu_set_wait_limit)
   // batch buffers
   nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, sfloor, nb_j, nb_r, nb_code, nb_cnt, nb_rev, orphans, G, dEdG, eatom, perm,
       type_count, W, force, energy, status, cell_cnt, cell_start, cell_atoms, atom_cell, mom, nb_t, tr_eref,
@@ -95,6 +96,8 @@ struct nnpgpu_ctx {
   cudaEvent_t prof_ev[NNPGPU_NSTAGES + 1] = {};
   double prof_ms[NNPGPU_NSTAGES] = {};
   long long prof_n[NNPGPU_NSTAGES] = {};
+  // nnpgpu_symm_noalloc: set-up done on this context (scratch address known, kernels loaded)
+  bool noalloc_ready = false;
 };
 
 namespace nnpgpu {

@@ -97,8 +97,9 @@ size_t type_sort_ints(int natoms);  // ints of the type_count buffer for a batch
 void launch_network_fp32(const BatchDev& B, const NetsP& N, int ntypes, int tile, cudaStream_t st);
 // stored FP64 descriptors (sstride per atom) into B.G (nin[t] values of each atom's type t)
 void launch_symm_load(const BatchDev& B, const int* nin, int ntypes, const double* src, int sstride, cudaStream_t st);
+// wait_limit: polls of each mbarrier wait before the kernel gives up with ERR_TIMEOUT
 int launch_network_bf16(const BatchDev& B, const NetsP& N, const void* tc_weights, int ntypes, cudaStream_t st, const void* tcnets_host,
-                        int want_grad);
+                        int want_grad, int wait_limit);
 // the energy trainer's batch error and parameter gradient after a batched energy pass
 int train_tiles(int natoms, int ntypes);
 int launch_train(const BatchDev& B, const NetsP& N, int ntypes, const double* eref, int loss, double delta, double* dcdo, double* err,

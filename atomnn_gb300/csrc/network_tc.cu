@@ -19,8 +19,10 @@
 // each GEMM's block is brought into shared memory by a 1-D TMA bulk copy (cp.async.bulk) into
 // one of two ping-pong buffers, the next GEMM's block loading while the current one runs.
 //
-// Every mbarrier wait is bounded; on timeout the kernel records ERR_TIMEOUT, stops issuing
-// work, waits (bounded) for its own MMAs and frees its TMEM before returning.
+// Every mbarrier wait is bounded (wait_limit polls, a kernel argument); on timeout the kernel
+// records ERR_TIMEOUT and stops issuing work.  Before it frees its TMEM and leaves, thread 0 waits
+// for every weight copy and MMA commit it issued and has not seen complete, bounded by
+// TC_DRAIN_LIMIT; if such a drain wait also runs out it records ERR_DRAIN.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -36,6 +38,7 @@ constexpr int TC_HMAX = 128;     // widest layer / padded input supported
 constexpr int TC_LMAX = 4;       // layers (hidden + output)
 
 constexpr int TC_GMAX = 2 * (TC_LMAX - 1);  // GEMMs per tile
+constexpr int TC_DRAIN_LIMIT = 1 << 22;     // polls of a drain wait (about half a second)
 // Per-species packed weights: GEMM g's B operand block [hi | lo] at blob offset off[g] with
 // bytes[g] bytes; g = 0..L-2 are the forward W_l (N=H_l, K=K_l), g = L-1.. the backward W_l^T
 // (N=K_l, K=H_l) for l = L-2 down to 0.
@@ -91,9 +94,9 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// bounded wait: false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (int it = 0; it < (1 << 22); ++it) {
+// bounded wait of at most limit polls: false on timeout (at once for limit 0)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int limit) {
+  for (int it = 0; it < limit; ++it) {
     if (mbar_try(bar, parity)) return true;
     if (it > 64) __nanosleep(128);
   }
@@ -183,7 +186,8 @@ __device__ __forceinline__ float act_d(int act, float a) {
 __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constant__ TcNetsP N, int ntypes, const int* __restrict__ tc,
                                                             const int* __restrict__ perm, const float* __restrict__ G, int gstride,
                                                             float* __restrict__ eatom, float* __restrict__ dEdG, int want_grad,
-                                                            uint32_t tmem_cols, int opk, int pcols, int* __restrict__ status) {
+                                                            uint32_t tmem_cols, int opk, int pcols, int wait_limit,
+                                                            int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   __shared__ uint64_t bar_w[2], bar_mma;
   __shared__ uint32_t tmem_slot;
@@ -225,9 +229,14 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
   const uint32_t t_acc = tmem;                      // accumulator columns [0, pcols)
   const uint32_t t_park = tmem + (uint32_t)pcols;   // parked derivatives, pcols columns per hidden layer
 
+  // thread 0's record of the asynchronous work it issued: a weight copy per buffer and the MMA
+  // commit, each with the barrier parity of its completion
+  bool w_pending[2] = {false, false}, mma_pending = false;
+  uint32_t w_par[2] = {0, 0}, mma_par = 0;
   // weights of GEMM g -> buffer g&1 by one 1-D TMA bulk copy, completion on bar_w[g&1]
   auto load_w = [&](int g) {
     if (g < ngemm) {
+      w_pending[g & 1] = true;
       uint64_t* bar = &bar_w[g & 1];
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(net.bytes[g]) : "memory");
       asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(wbuf[g & 1])),
@@ -256,12 +265,16 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
   fence_async_smem();
   __syncthreads();
 
-  uint32_t mma_phase = 0, wphase[2] = {0, 0};
   // GEMM g: D[128 x n] = A[128 x k] * B[n x k]^T with split operands; all threads return after
   // the MMAs completed (or a timeout was recorded); then the next-but-one weights are requested.
   auto gemm = [&](int g, int n, int k) {
     if (s_err == 0 && tid == 0) {
-      if (!mbar_wait(&bar_w[g & 1], wphase[g & 1])) s_err = 1;
+      if (mbar_wait(&bar_w[g & 1], w_par[g & 1], wait_limit)) {
+        w_pending[g & 1] = false;
+        w_par[g & 1] ^= 1u;
+      } else {
+        s_err = 1;
+      }
       tc_fence_after();
       if (s_err == 0) {
         const uint32_t idesc = umma_idesc(TC_M, n);
@@ -275,12 +288,16 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
           tc_mma(t_acc, umma_desc(ah + o, k), umma_desc(bl + o, k), idesc, 1u);
         }
         tc_commit(&bar_mma);
-        if (!mbar_wait(&bar_mma, mma_phase)) s_err = 1;
+        mma_pending = true;
+        if (mbar_wait(&bar_mma, mma_par, wait_limit)) {
+          mma_pending = false;
+          mma_par ^= 1u;
+        } else {
+          s_err = 1;
+        }
       }
       if (s_err == 0) load_w(g + 2);  // buffer g&1 is free again
     }
-    wphase[g & 1] ^= 1u;
-    mma_phase ^= 1u;
     __syncthreads();
     tc_fence_after();
   };
@@ -352,10 +369,14 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
       __syncthreads();
     }
   }
-  if (s_err && tid == 0) atomicOr(&status[ST_ERROR], ERR_TIMEOUT);
-  // outstanding weight copies must land before the CTA exits (bounded)
-  if (tid == 0 && !s_err) {
-    for (int q = g; q < ngemm && q < g + 2; ++q) mbar_wait(&bar_w[q & 1], wphase[q & 1]);
+  // every copy and MMA this CTA issued lands before its shared memory and TMEM are released
+  if (tid == 0) {
+    bool drained = true;
+    for (int b = 0; b < 2; ++b)
+      if (w_pending[b]) drained = mbar_wait(&bar_w[b], w_par[b], TC_DRAIN_LIMIT) && drained;
+    if (mma_pending) drained = mbar_wait(&bar_mma, mma_par, TC_DRAIN_LIMIT) && drained;
+    if (s_err) atomicOr(&status[ST_ERROR], ERR_TIMEOUT);
+    if (!drained) atomicOr(&status[ST_ERROR], ERR_DRAIN);
   }
   tc_fence_before();
   __syncthreads();
@@ -464,7 +485,7 @@ int prepare_tc_weights(nnpgpu_ctx* c) {
 }
 
 int launch_network_bf16(const BatchDev& B, const NetsP&, const void* tc, int ntypes, cudaStream_t st, const void* tcnets_host,
-                        int want_grad) {
+                        int want_grad, int wait_limit) {
   if (!tc || !tcnets_host) return -1;
   if (B.natoms == 0) return 0;
   const TcNetsP& N = *reinterpret_cast<const TcNetsP*>(tcnets_host);
@@ -494,7 +515,7 @@ int launch_network_bf16(const BatchDev& B, const NetsP&, const void* tc, int nty
   }
   const int tiles = (B.natoms + TC_M - 1) / TC_M + ntypes;
   network_tc_kernel<<<tiles, 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride, B.eatom, B.dEdG, want_grad, cols,
-                                             opk, pcols, B.status);
+                                             opk, pcols, wait_limit, B.status);
   return 0;
 }
 

@@ -156,10 +156,16 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
   const double* R2 = col[perm[2]];
   const double cx[3] = {R0[1] * R1[2] - R0[2] * R1[1], R0[2] * R1[0] - R0[0] * R1[2], R0[0] * R1[1] - R0[1] * R1[0]};
   const double dot2 = R2[0] * cx[0] + R2[1] * cx[1] + R2[2] * cx[2];
+  // shell ratios bounded in FP64 before the integer conversion: a near-flat cell gives huge ratios
+  const double ratio[3] = {2.0 * rc / nrm3(R0), 2.0 * rc / (nrm3(cx) / nrm3(R0)), 2.0 * rc / std::fabs(dot2 / (nrm3(R0) * nrm3(R1)))};
   int shell[3];
-  shell[0] = (int)std::floor(2.0 * rc / nrm3(R0));
-  shell[1] = (int)std::floor(2.0 * rc / (nrm3(cx) / nrm3(R0)));
-  shell[2] = (int)std::floor(2.0 * rc / std::fabs(dot2 / (nrm3(R0) * nrm3(R1))));
+  double nimg_total = 1;
+  for (int c = 0; c < 3; ++c) {
+    if (!std::isfinite(ratio[c]) || ratio[c] > 1e6) throw PotError(NNPGPU_ERR_INVALID, "cell too thin for the cutoff (lattice image shells)");
+    shell[c] = (int)std::floor(ratio[c]);
+    nimg_total *= 2.0 * shell[c] + 1;
+  }
+  if (nimg_total > 1e6) throw PotError(NNPGPU_ERR_INVALID, "cell too thin for the cutoff: more than 1e6 lattice images");
   double Lsum = nrm3(col[0]) + nrm3(col[1]) + nrm3(col[2]);
   m.margin = (float)(2.0 * rc * (Lsum * 1e-6 + 1e-5) + 1e-4 * rc * rc);
   if (shell[0] == 0 && shell[1] == 0 && shell[2] == 0) {
@@ -226,7 +232,7 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
     launch_type_sort(B, c->pot.ntypes, st);
     if (flags & NNPGPU_BF16) {
       const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st, c->tcnets ? c->tcnets->data() : nullptr,
-                                            want_force ? 1 : 0);
+                                            want_force ? 1 : 0, c->tc_wait_limit);
       if (rcode == -1) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "BF16 network path unavailable for this potential");
       if (rcode != 0) return cuda_fail(c, cudaGetLastError(), "tensor-core network set-up");
     } else {
@@ -481,6 +487,10 @@ int check_status(nnpgpu_ctx* c, const int* st_words, int cap) {
   }
   if (st_words[ST_ERROR] & ERR_BAD_POSITION) return set_error(c, NNPGPU_ERR_INVALID, "non-finite atom position");
   if (st_words[ST_ERROR] & ERR_BAD_TYPE) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
+  if (st_words[ST_ERROR] & ERR_DRAIN)
+    return set_error(c, NNPGPU_ERR_TIMEOUT,
+                     "a bounded wait on the device ran out and the kernel's own copies did not finish either (tensor-core network); "
+                     "destroy this context");
   if (st_words[ST_ERROR] & ERR_TIMEOUT) return set_error(c, NNPGPU_ERR_TIMEOUT, "a bounded wait on the device ran out (tensor-core network)");
   if (st_words[ST_ERROR] & ERR_ORPHANS) return set_error(c, NNPGPU_ERR_INVALID, "inconsistent neighbour lists (too many unmatched minimum images)");
   if (st_words[ST_MAXCOUNT] > cap) {
@@ -910,6 +920,15 @@ extern "C" int nnpgpu_autotune(nnpgpu_ctx* c, int nstruc, const int* natoms, con
   return NNPGPU_OK;
 }
 
+extern "C" int nnpgpu_set_wait_limit(nnpgpu_ctx* c, int polls) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (polls < 0) return set_error(c, NNPGPU_ERR_INVALID, "wait limit: polls must be >= 0");
+  c->tc_wait_limit = polls;
+  drop_graphs(c);  // captured sequences hold the old limit
+  c->shapes_seen.clear();
+  return NNPGPU_OK;
+}
+
 extern "C" int nnpgpu_get_tune(const nnpgpu_ctx* c, int* warps_nbr, int* warps_symm, int* warps_force, int* nn_tile) {
   if (!c) return NNPGPU_ERR_INVALID;
   if (warps_nbr) *warps_nbr = c->tune.warps_nbr;
@@ -1149,7 +1168,8 @@ extern "C" int nnpgpu_energy_symm(nnpgpu_ctx* c, int nstruc, const int* natoms, 
   launch_symm_load(B, c->P.nin, c->pot.ntypes, (const double*)c->symm_in.p, symm_stride, st);
   launch_type_sort(B, c->pot.ntypes, st);
   if (flags & NNPGPU_BF16) {
-    const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st, c->tcnets ? c->tcnets->data() : nullptr, 0);
+    const int rcode = launch_network_bf16(B, c->nets, c->tcbuf, c->pot.ntypes, st, c->tcnets ? c->tcnets->data() : nullptr, 0,
+                                          c->tc_wait_limit);
     if (rcode == -1) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "BF16 network path unavailable for this potential");
     if (rcode != 0) return cuda_fail(c, cudaGetLastError(), "tensor-core network set-up");
   } else {

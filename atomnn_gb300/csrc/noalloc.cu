@@ -4,9 +4,10 @@
 // that divides the GPU's memory among its own pools before the first step, or a service that
 // reserves all device memory at start-up and forbids allocation afterwards (an allocation in
 // the middle of a step could fail, or synchronise the device at a point the caller does not
-// control).  nnpgpu_symm_noalloc serves them: it computes NNP::symm for one structure whose
-// inputs and outputs the caller provides in device memory, and keeps every intermediate
-// (geometry, neighbour lists, status words) in one scratch array compiled into this library.
+// control).  nnpgpu_symm_noalloc serves them: it computes the symmetry functions of one
+// structure whose inputs and outputs the caller provides in device memory, and keeps every
+// intermediate (geometry, neighbour lists, status words) in one scratch array compiled into
+// this library.
 //
 // Limits: at most NOALLOC_MAX_ATOMS atoms, NOALLOC_CAP neighbours per atom within the cutoff,
 // NOALLOC_MAX_IMAGES lattice images; larger requests are rejected with a message.  The array
@@ -14,6 +15,13 @@
 // share it: the status words and the atom->structure map are cleared at the start of each call,
 // the rest is overwritten; calls whose work overlaps on the GPU (two streams, two host threads)
 // race on it and must be serialised by the caller.
+//
+// Set-up: the first call on a context (natoms = 0 is enough) looks up the array's device address
+// with the context's device current and runs the three kernels of this entry point once on a
+// one-atom structure held in the array.  CUDA loads modules and kernels lazily (the default since
+// CUDA 12.2), and loading places code and the array in device memory; after the set-up call the
+// later calls load nothing.  Make the set-up call before reserving the device's memory and
+// before any stream capture.
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -26,10 +34,11 @@ namespace {
 constexpr int NOALLOC_MAX_ATOMS = 1024;
 constexpr int NOALLOC_CAP = 192;
 constexpr int NOALLOC_MAX_IMAGES = 512;
+constexpr int NOALLOC_WARM_NIN = 1024;  // output row of the set-up call (>= any input size)
 
 // Layout of the scratch array (offsets in bytes, each 256-byte aligned).
 struct ScratchLayout {
-  size_t meta, imgs, status, atom_struc, sfrac, sfloor, nb_cnt, nb_j, nb_r, nb_code, total;
+  size_t meta, imgs, status, atom_struc, sfrac, sfloor, nb_cnt, nb_j, nb_r, nb_code, warm_posn, warm_type, warm_symm, total;
 };
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr ScratchLayout make_layout() {
@@ -45,6 +54,9 @@ constexpr ScratchLayout make_layout() {
   L.nb_j = o; o = align256(o + sizeof(int) * NOALLOC_MAX_ATOMS * NOALLOC_CAP);
   L.nb_r = o; o = align256(o + sizeof(float4) * NOALLOC_MAX_ATOMS * NOALLOC_CAP);
   L.nb_code = o; o = align256(o + sizeof(int) * NOALLOC_MAX_ATOMS * NOALLOC_CAP);
+  L.warm_posn = o; o = align256(o + sizeof(double) * 3);  // the set-up call's one-atom structure
+  L.warm_type = o; o = align256(o + sizeof(int));
+  L.warm_symm = o; o = align256(o + sizeof(float) * NOALLOC_WARM_NIN);
   L.total = o;
   return L;
 }
@@ -71,6 +83,19 @@ int scratch_address(nnpgpu_ctx* c, void** out) {
   *out = g_scratch_addr[c->device];
   return NNPGPU_OK;
 }
+
+// Makes the context's device current for the call and gives the caller's device back on return.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int now = -1;
+    if (prev >= 0 && cudaGetDevice(&now) == cudaSuccess && now != prev) cudaSetDevice(prev);
+  }
+};
 
 double nrm3(const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 
@@ -136,17 +161,21 @@ int fixed_meta(const double* cell, int natoms, double rc, StrucMeta& m, ImgEntry
   const double* R2 = col[perm[2]];
   const double cx[3] = {R0[1] * R1[2] - R0[2] * R1[1], R0[2] * R1[0] - R0[0] * R1[2], R0[0] * R1[1] - R0[1] * R1[0]};
   const double dot2 = R2[0] * cx[0] + R2[1] * cx[1] + R2[2] * cx[2];
+  // shell ratios in FP64, bounded before the integer conversion (a near-flat cell gives huge ratios)
+  const double ratio[3] = {2.0 * rc / nrm3(R0), 2.0 * rc / (nrm3(cx) / nrm3(R0)), 2.0 * rc / std::fabs(dot2 / (nrm3(R0) * nrm3(R1)))};
+  long long want = 1;
   int shell[3];
-  shell[0] = (int)std::floor(2.0 * rc / nrm3(R0));
-  shell[1] = (int)std::floor(2.0 * rc / (nrm3(cx) / nrm3(R0)));
-  shell[2] = (int)std::floor(2.0 * rc / std::fabs(dot2 / (nrm3(R0) * nrm3(R1))));
+  for (int q = 0; q < 3; ++q) {
+    if (!std::isfinite(ratio[q]) || ratio[q] > (double)NOALLOC_MAX_IMAGES) return -2;
+    shell[q] = (int)std::floor(ratio[q]);
+    want *= 2LL * shell[q] + 1;
+  }
   const double Lsum = nrm3(col[0]) + nrm3(col[1]) + nrm3(col[2]);
   m.margin = (float)(2.0 * rc * (Lsum * 1e-6 + 1e-5) + 1e-4 * rc * rc);
   if (shell[0] == 0 && shell[1] == 0 && shell[2] == 0) {
     m.mode = 2;
     return 0;
   }
-  const long long want = (long long)(2 * shell[0] + 1) * (2 * shell[1] + 1) * (2 * shell[2] + 1);
   if (want > NOALLOC_MAX_IMAGES) return -2;
   m.mode = 1;
   set_image_box(m, inv, rc, shell, perm);
@@ -167,47 +196,10 @@ int fixed_meta(const double* cell, int natoms, double rc, StrucMeta& m, ImgEntry
   return 0;
 }
 
-}  // namespace
-}  // namespace nnpgpu
-
-using namespace nnpgpu;
-
-// Symmetry functions of one structure without device allocation (see the header for the
-// contract).  The first call on a device looks up the scratch array's device address; make
-// that first call before any stream capture.
-extern "C" int nnpgpu_symm_noalloc(nnpgpu_ctx* c, int natoms, const double* d_posn, const int* d_species, const double* cell,
-                                   float* d_symm, int symm_stride, void* stream) {
-  if (!c) return NNPGPU_ERR_INVALID;
-  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
-  if (natoms < 0 || natoms > NOALLOC_MAX_ATOMS)
-    return set_error(c, NNPGPU_ERR_INVALID,
-                     "nnpgpu_symm_noalloc: " + std::to_string(natoms) + " atoms, the limit is " + std::to_string(NOALLOC_MAX_ATOMS));
-  if (natoms > 0 && (!d_posn || !d_species || !d_symm))
-    return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: device input or output pointer missing");
-  if (symm_stride < c->max_nin)
-    return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: symm_stride below the largest input size");
-  cudaSetDevice(c->device);
-  void* base = nullptr;
-  const int rc0 = scratch_address(c, &base);
-  if (rc0 != NNPGPU_OK) return rc0;
-  if (natoms == 0) return NNPGPU_OK;
-  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-
-  StrucMeta meta;
-  ImgEntry imgs[NOALLOC_MAX_IMAGES];
-  int nimg = 0;
-  const int g = fixed_meta(cell, natoms, c->pot.rc, meta, imgs, nimg);
-  if (g == -1) return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: singular or non-finite cell");
-  if (g == -2)
-    return set_error(c, NNPGPU_ERR_INVALID,
-                     "nnpgpu_symm_noalloc: the cell needs more than " + std::to_string(NOALLOC_MAX_IMAGES) + " lattice images");
-  uint8_t* S = (uint8_t*)base;
-  // pageable-source copies return once the stack buffers have been consumed
-  cudaMemcpyAsync(S + kLayout.meta, &meta, sizeof(meta), cudaMemcpyHostToDevice, st);
-  if (nimg > 0) cudaMemcpyAsync(S + kLayout.imgs, imgs, sizeof(ImgEntry) * nimg, cudaMemcpyHostToDevice, st);
-  cudaMemsetAsync(S + kLayout.status, 0, sizeof(int) * ST_WORDS, st);
-  cudaMemsetAsync(S + kLayout.atom_struc, 0, sizeof(int) * natoms, st);
-
+// Launches the entry point's kernels on one structure whose geometry is already in the scratch
+// array at base (meta, images, cleared status and atom->structure words).
+int run_symm(nnpgpu_ctx* c, uint8_t* S, int natoms, const double* d_posn, const int* d_species, float* d_symm, int symm_stride,
+             cudaStream_t st) {
   BatchDev B;
   B.natoms = natoms;
   B.nstruc = 1;
@@ -231,11 +223,86 @@ extern "C" int nnpgpu_symm_noalloc(nnpgpu_ctx* c, int natoms, const double* d_po
   launch_neighbors(B, st);
   if (launch_symm(B, c->P, c->ne, c->nz, c->tune.warps_symm, st) != 0)
     return set_error(c, NNPGPU_ERR_UNSUPPORTED, "no descriptor kernel for this potential");
-  cudaError_t e = cudaGetLastError();
+  const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(c, NNPGPU_ERR_CUDA, std::string("nnpgpu_symm_noalloc launch: ") + cudaGetErrorString(e));
+  return NNPGPU_OK;
+}
+
+// Copies one structure's geometry into the scratch array and clears the words that must start at zero.
+void upload_geometry(uint8_t* S, const StrucMeta& meta, const ImgEntry* imgs, int nimg, int natoms, cudaStream_t st) {
+  // pageable-source copies return once the stack buffers have been consumed
+  cudaMemcpyAsync(S + kLayout.meta, &meta, sizeof(meta), cudaMemcpyHostToDevice, st);
+  if (nimg > 0) cudaMemcpyAsync(S + kLayout.imgs, imgs, sizeof(ImgEntry) * nimg, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(S + kLayout.status, 0, sizeof(int) * ST_WORDS, st);
+  cudaMemsetAsync(S + kLayout.atom_struc, 0, sizeof(int) * natoms, st);
+}
+
+// First call on a context: the array's device address, then one pass of the kernels over a
+// single atom at the origin with no cell (species 0, output row in the array), so that every
+// kernel this entry point launches for the context's potential is loaded on the device.
+int setup(nnpgpu_ctx* c, uint8_t** base) {
+  void* p = nullptr;
+  int rc = scratch_address(c, &p);
+  if (rc != NNPGPU_OK) return rc;
+  *base = (uint8_t*)p;
+  if (c->noalloc_ready) return NNPGPU_OK;
+  if (c->max_nin > NOALLOC_WARM_NIN) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "nnpgpu_symm_noalloc: input size above 1024");
+  uint8_t* S = *base;
+  cudaStream_t st = c->stream;
+  StrucMeta meta;
+  int nimg = 0;
+  fixed_meta(nullptr, 1, c->pot.rc, meta, nullptr, nimg);
+  upload_geometry(S, meta, nullptr, 0, 1, st);
+  cudaMemsetAsync(S + kLayout.warm_posn, 0, sizeof(double) * 3, st);
+  cudaMemsetAsync(S + kLayout.warm_type, 0, sizeof(int), st);
+  rc = run_symm(c, S, 1, (const double*)(S + kLayout.warm_posn), (const int*)(S + kLayout.warm_type), (float*)(S + kLayout.warm_symm),
+                c->max_nin, st);
+  if (rc != NNPGPU_OK) return rc;
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return set_error(c, NNPGPU_ERR_CUDA, std::string("nnpgpu_symm_noalloc set-up: ") + cudaGetErrorString(e));
+  c->noalloc_ready = true;
+  return NNPGPU_OK;
+}
+
+}  // namespace
+}  // namespace nnpgpu
+
+using namespace nnpgpu;
+
+// Symmetry functions of one structure without device allocation (see the header for the
+// contract).  The first call on a context does the set-up described at the top of this file.
+extern "C" int nnpgpu_symm_noalloc(nnpgpu_ctx* c, int natoms, const double* d_posn, const int* d_species, const double* cell,
+                                   float* d_symm, int symm_stride, void* stream) {
+  if (!c) return NNPGPU_ERR_INVALID;
+  if (!c->stream) return set_error(c, NNPGPU_ERR_CUDA, "context has no device");
+  if (natoms < 0 || natoms > NOALLOC_MAX_ATOMS)
+    return set_error(c, NNPGPU_ERR_INVALID,
+                     "nnpgpu_symm_noalloc: " + std::to_string(natoms) + " atoms, the limit is " + std::to_string(NOALLOC_MAX_ATOMS));
+  if (natoms > 0 && (!d_posn || !d_species || !d_symm))
+    return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: device input or output pointer missing");
+  if (natoms > 0 && symm_stride < c->max_nin)
+    return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: symm_stride below the largest input size");
+  DeviceGuard guard(c->device);
+  uint8_t* S = nullptr;
+  const int rc0 = setup(c, &S);
+  if (rc0 != NNPGPU_OK) return rc0;
+  if (natoms == 0) return NNPGPU_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+
+  StrucMeta meta;
+  ImgEntry imgs[NOALLOC_MAX_IMAGES];
+  int nimg = 0;
+  const int g = fixed_meta(cell, natoms, c->pot.rc, meta, imgs, nimg);
+  if (g == -1) return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: singular or non-finite cell");
+  if (g == -2)
+    return set_error(c, NNPGPU_ERR_INVALID,
+                     "nnpgpu_symm_noalloc: the cell needs more than " + std::to_string(NOALLOC_MAX_IMAGES) + " lattice images");
+  upload_geometry(S, meta, imgs, nimg, natoms, st);
+  const int rc1 = run_symm(c, S, natoms, d_posn, d_species, d_symm, symm_stride, st);
+  if (rc1 != NNPGPU_OK) return rc1;
   int hstat[ST_WORDS];
   cudaMemcpyAsync(hstat, S + kLayout.status, sizeof(hstat), cudaMemcpyDeviceToHost, st);
-  e = cudaStreamSynchronize(st);
+  const cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return set_error(c, NNPGPU_ERR_CUDA, std::string("nnpgpu_symm_noalloc: ") + cudaGetErrorString(e));
   if (hstat[ST_ERROR] & ERR_BAD_POSITION) return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: non-finite atom position");
   if (hstat[ST_ERROR] & ERR_BAD_TYPE) return set_error(c, NNPGPU_ERR_INVALID, "nnpgpu_symm_noalloc: species index out of range");

@@ -18,7 +18,7 @@ ENERGY, FORCE, SYMM, BF16, NO_VACUUM, BATCHED = 0x1, 0x2, 0x4, 0x8, 0x10, 0x20
 EXPORTS = ["nnpgpu_create", "nnpgpu_destroy", "nnpgpu_last_error", "nnpgpu_ntypes", "nnpgpu_type_index", "nnpgpu_cutoff",
            "nnpgpu_ninput", "nnpgpu_compute", "nnpgpu_compute_device", "nnpgpu_neighbors", "nnpgpu_neighbors_rc", "nnpgpu_serve_start", "nnpgpu_submit",
            "nnpgpu_poll", "nnpgpu_serve_stop", "nnpgpu_profile_enable", "nnpgpu_profile_read",
-           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
+           "nnpgpu_profile_stage_name", "nnpgpu_symm_noalloc", "nnpgpu_autotune", "nnpgpu_get_tune", "nnpgpu_set_tune", "nnpgpu_set_wait_limit", "nnpgpu_md_create", "nnpgpu_md_forces", "nnpgpu_md_run",
            "nnpgpu_md_state", "nnpgpu_md_destroy", "nnpgpu_nparams", "nnpgpu_train_grad", "nnpgpu_energy_symm",
            "nnpgpu_train_force_grad", "nnpgpu_get_params", "nnpgpu_set_params", "nnpgpu_write_potential"]
 
@@ -67,6 +67,7 @@ def load_library(path=LIB_PATH):
     L.nnpgpu_autotune.argtypes = [vp, ip, vp, vp, vp, vp, ip, ctypes.c_char_p, ip]
     L.nnpgpu_get_tune.argtypes = [vp, vp, vp, vp, vp]
     L.nnpgpu_set_tune.argtypes = [vp, ip, ip, ip, ip]
+    L.nnpgpu_set_wait_limit.argtypes = [vp, ip]
     L.nnpgpu_md_create.argtypes = [vp, ip, vp, vp, vp, vp, vp, dp, dp, ip, ctypes.POINTER(vp)]
     L.nnpgpu_md_forces.argtypes = [vp, vp]
     L.nnpgpu_md_run.argtypes = [vp, ip, vp, vp]
@@ -193,6 +194,10 @@ class Engine:
 
     def set_tune(self, warps_nbr=4, warps_symm=4, warps_force=4, nn_tile=32):
         self._check(self.lib.nnpgpu_set_tune(self._ctx, warps_nbr, warps_symm, warps_force, nn_tile))
+
+    def set_wait_limit(self, polls=1 << 22):
+        """nnpgpu_set_wait_limit: polls of each mbarrier wait of the tensor-core networks."""
+        self._check(self.lib.nnpgpu_set_wait_limit(self._ctx, polls))
 
     # ---- training: batch error and parameter gradient of the energy loss
     LOSS = {"MSE": 0, "MAE": 1, "HUBER": 2, "ASINH": 3}

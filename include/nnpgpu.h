@@ -96,19 +96,24 @@ int nnpgpu_neighbors(nnpgpu_ctx* ctx, int natoms, const double* posn, const doub
 int nnpgpu_neighbors_rc(nnpgpu_ctx* ctx, double rc, int natoms, const double* posn, const double* cell,
                         int cap, int* count, int* index, float* r, unsigned char* min, int* shift);
 
-/* ---- symmetry functions without device allocation.  No counterpart in the reference (AtomNN
- * allocates through Eigen on every call).  For callers that cannot let a library allocate device
- * memory while they run: codes that divide the GPU's memory among their own pools before the
- * first step, and services that reserve all device memory at start-up.  Computes NNP::symm
- * (src/nnp/nnp.cpp:334-381) of one structure of at most 1024 atoms with at most 192 neighbours per
- * atom and 512 lattice images, keeping every intermediate in a 4.6 MB scratch array compiled into
- * the library (each GPU that loads the library holds it until the process exits).
+/* ---- symmetry functions without device allocation.  This entry point has no counterpart in the
+ * reference.  It is for callers that cannot let a library allocate device memory while they run:
+ * codes that divide the GPU's memory among their own pools before the first step, and services
+ * that reserve all device memory at start-up, where an allocation in the middle of a step could
+ * fail or synchronise the device at a point the caller does not control.  It computes the same
+ * symmetry functions as nnpgpu_compute with NNPGPU_SYMM, for one structure of at most 1024 atoms
+ * with at most 192 neighbours per atom and 512 lattice images, and keeps every intermediate in a
+ * 4.6 MB scratch array compiled into the library (each GPU that loads the library holds it until
+ * the process exits).  It calls no cudaMalloc, cudaFree or allocating library routine.
  * d_posn (natoms*3 FP64), d_species and d_symm (natoms rows of symm_stride FP32, symm_stride >= the
  * largest nnpgpu_ninput) are device pointers; cell is a host array as in nnpgpu_compute.  Returns
  * after the work on stream (NULL = the context's stream) has finished.  Larger requests are
- * rejected with NNPGPU_ERR_INVALID or NNPGPU_ERR_CAPACITY and a message.  The first call on a
- * device looks up the scratch array's address: make that call before any stream capture.  All
- * calls share the scratch array, so calls whose work overlaps on the GPU race on it. */
+ * rejected with NNPGPU_ERR_INVALID or NNPGPU_ERR_CAPACITY and a message.
+ * Set-up: the first call on a context (natoms = 0 is enough) looks up the scratch array's device
+ * address and loads the kernels this entry point launches (CUDA loads them lazily, and loading
+ * places code in device memory); make that call before reserving the device's memory and before
+ * any stream capture.  All calls share the scratch array, so calls whose work overlaps on the GPU
+ * race on it: serialise them.  The caller's current device is left as it was. */
 int nnpgpu_symm_noalloc(nnpgpu_ctx* ctx, int natoms, const double* d_posn, const int* d_species, const double* cell,
                         float* d_symm, int symm_stride, void* stream);
 
@@ -174,6 +179,14 @@ int nnpgpu_autotune(nnpgpu_ctx* ctx, int nstruc, const int* natoms, const double
                     const double* cell, int flags, char* report, int report_len);
 int nnpgpu_get_tune(const nnpgpu_ctx* ctx, int* warps_nbr, int* warps_symm, int* warps_force, int* nn_tile);
 int nnpgpu_set_tune(nnpgpu_ctx* ctx, int warps_nbr, int warps_symm, int warps_force, int nn_tile);
+
+/* ---- failure detection (no counterpart in the reference, which has no device waits).  Bound on
+ * each mbarrier wait of the tensor-core network kernel (NNPGPU_BF16), in polls; the default
+ * 4194304 is about half a second.  A wait that runs out ends the call with NNPGPU_ERR_TIMEOUT after
+ * the kernel has waited (bounded) for the copies and MMAs it issued and freed its TMEM, so the
+ * context stays usable; if those did not finish either the message says to destroy the context.
+ * 0 makes every wait give up at once (a test of this path). */
+int nnpgpu_set_wait_limit(nnpgpu_ctx* ctx, int polls);
 
 /* ---- serving: continuous batching of energy+force requests (no counterpart in the
  * reference, whose compute tool evaluates a fixed file list; it serves the same call as
