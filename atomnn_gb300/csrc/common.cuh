@@ -46,12 +46,14 @@ struct RadialP {
 // |lambda| <= 1); its moments start at float moff of the atom's row.  tab is the block's offset
 // in PotParams::atab: n grid cells (as floats), then for a moment block the n x (ne*(MOM_N+1))
 // matrix M[f][e*(MOM_N+1)+k] = norm * (coefficient of cos^k in function f's angular term) when f
-// has width e, 0 otherwise.
+// has width e, 0 otherwise.  fn = 1 marks a block that leaves the grid (a zeta that is not a
+// power of two up to 2^(NZ_MAX-1), more than NE_MAX widths or NL lambdas): it takes the
+// per-function triplet path, and tab holds per function (1/eta^alpha, lambda, zeta, 0).
 struct AngP {
   int n, off, cut, alpha;
   float rc, pirc, rci, norm;
   int ne, nl, nz, mom;
-  int moff, phi, tab, pad2;
+  int moff, phi, tab, fn;
   float ietap[NE_MAX];
   float lam[NL];
   signed char gidx[NA_MAX];

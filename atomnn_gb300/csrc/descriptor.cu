@@ -450,7 +450,7 @@ __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, co
 template <bool GEN>
 __device__ void block_pair_factors(const WarpSmem& S, const AngP& A, int lo, int hi, int cap, bool with_fc) {
   const int lane = threadIdx.x & 31;
-  const bool sum = GEN && ang_sum_family(A.phi);
+  const bool sum = GEN && (ang_sum_family(A.phi) || A.fn);
   for (int p = lo + lane; p < hi; p += 32) {
     const float d = S.d[p];
     float f, g;
@@ -837,6 +837,129 @@ __device__ void force_block_gen(const WarpSmem& S, const AngP& A, const Sched& s
   }
 }
 
+// ------------------------------------------------------------------ per-function angular blocks
+// Blocks that leave the (width) x (lambda) x (2^m) grid (AngP::fn: a real zeta, more than NE_MAX
+// widths or NL lambdas) evaluate every function per triplet, as BasisA::symm and BasisA::force do
+// (basis_angular.cpp:406-640): pow(|(1 + lambda cos)/2|, zeta) times the family's radial factor
+// from ex[p] = r_p^alpha and the cutoffs.  Linked only into the GEN kernel instances.
+constexpr int FN_CHUNK = 8;  // functions accumulated per walk over the block's triplets
+
+// radial factor of one function: product families h(ie r_a^alpha) h(ie r_b^alpha), sum families
+// and GAUSS functions of ie (r_a^alpha + r_b^alpha); ka, kb the derivative weights of ang_h
+__device__ __forceinline__ float fn_radial(int phi, float ie, float da, float db, float& ka, float& kb) {
+  if (phi == ANG_IPOWP || phi == ANG_SECHP) {
+    const float ha = ang_h(phi, ie * da, ka);
+    const float hb = ang_h(phi, ie * db, kb);
+    return ha * hb;
+  }
+  const float h = ang_h(phi, ie * (da + db), ka);
+  kb = ka;
+  return h;
+}
+
+// G4 of a per-function block: FN_CHUNK functions per walk, written to Gi (times the norm).
+__device__ void symm_block_fn(const WarpSmem& S, const AngP& A, const float* __restrict__ ftab, const Sched& sc, float* Gi) {
+  const int lane = threadIdx.x & 31;
+  for (int f0 = 0; f0 < A.n; f0 += FN_CHUNK) {
+    float ie[FN_CHUNK], lam[FN_CHUNK], zeta[FN_CHUNK], acc[FN_CHUNK];
+#pragma unroll
+    for (int k = 0; k < FN_CHUNK; ++k) {
+      const int f = min(f0 + k, A.n - 1);
+      ie[k] = ftab[4 * f];
+      lam[k] = ftab[4 * f + 1];
+      zeta[k] = ftab[4 * f + 2];
+      acc[k] = 0.f;
+    }
+    for (int q = 0; q * 32 < sc.nown; ++q) {
+      const int x = q * 32 + lane;
+      const int a = sc.xb + min(x, sc.nown - 1);
+      const float uax = S.ux[a], uay = S.uy[a], uaz = S.uz[a], da = S.ex[a], fa = S.fc[a];
+      for (int dd = sc.d0; dd <= sc.d1; ++dd) {
+        const int nx = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+        if (x < nx) {
+          int y = x + dd;
+          if (y >= sc.mod) y -= sc.mod;
+          const int b = sc.yb + y;
+          const float cs = uax * S.ux[b] + uay * S.uy[b] + uaz * S.uz[b];
+          const float fab = fa * S.fc[b], db = S.ex[b];
+#pragma unroll
+          for (int k = 0; k < FN_CHUNK; ++k) {
+            float ka, kb;
+            const float R = fn_radial(A.phi, ie[k], da, db, ka, kb);
+            acc[k] = fmaf(powf(fabsf(0.5f * (1.0f + lam[k] * cs)), zeta[k]), R * fab, acc[k]);
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < FN_CHUNK; ++k) {
+      const float v = warp_sum(acc[k]);
+      if (lane == 0 && f0 + k < A.n) Gi[A.off + f0 + k] = A.norm * v;
+    }
+  }
+}
+
+// Chain rule of a per-function block: per triplet the sums over the block's functions of
+// BasisA::force (basis_angular.cpp:456-640) with cw = |(1 + lambda cos)/2| and s = dE/dG_f:
+//   Q = sum s R cw^zeta,  Q2a/b = sum s ie k_a/b R cw^zeta,  Pp = sum s R lambda zeta cw^(zeta-1),
+// then phi, eta0, eta1 and the slot vectors as in force_block_gen.
+__device__ void force_block_fn(const WarpSmem& S, const AngP& A, const float* __restrict__ ftab, const Sched& sc, const float* gi) {
+  const int lane = threadIdx.x & 31;
+  const float hn = -0.5f * A.norm, nn = -A.norm;
+  const float* __restrict__ sf = gi + A.off;
+  for (int q = 0; q * 32 < sc.nown; ++q) {
+    const int x = q * 32 + lane;
+    const int a = sc.xb + min(x, sc.nown - 1);
+    const float uax = S.ux[a], uay = S.uy[a], uaz = S.uz[a], da = S.ex[a];
+    const float fa = S.fc[a], ga = S.gc[a], pa = S.dpa[a], ia = S.inv[a];
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f;
+    for (int dd = sc.d0; dd <= sc.d1; ++dd) {
+      const int nx = (sc.tri && 2 * dd == sc.nJ) ? (sc.nJ >> 1) : sc.nown;
+      if (x < nx) {
+        int y = x + dd;
+        if (y >= sc.mod) y -= sc.mod;
+        const int b = sc.yb + y;
+        const float ubx = S.ux[b], uby = S.uy[b], ubz = S.uz[b], db = S.ex[b];
+        const float fb = S.fc[b], gb = S.gc[b], pb = S.dpa[b], ib = S.inv[b];
+        const float cs = uax * ubx + uay * uby + uaz * ubz;
+        float Q = 0.f, Q2a = 0.f, Q2b = 0.f, Pp = 0.f;
+#pragma unroll 2
+        for (int f = 0; f < A.n; ++f) {
+          const float ie = ftab[4 * f], lam = ftab[4 * f + 1], zeta = ftab[4 * f + 2];
+          float ka, kb;
+          const float R = fn_radial(A.phi, ie, da, db, ka, kb);
+          const float cw = fabsf(0.5f * (1.0f + lam * cs));
+          const float cz1 = powf(cw, zeta - 1.0f);
+          const float sR = sf[f] * R;
+          const float qe = sR * cw * cz1;
+          Q += qe;
+          Q2a = fmaf(ie * ka, qe, Q2a);
+          Q2b = fmaf(ie * kb, qe, Q2b);
+          Pp = fmaf(sR, lam * zeta * cz1, Pp);
+        }
+        const float phi = hn * fa * fb * Pp;
+        const float eta0 = nn * fb * (ga * Q - pa * Q2a);
+        const float eta1 = nn * fa * (gb * Q - pb * Q2b);
+        const float Aa = -phi * cs * ia + eta0, Ba = phi * ia;
+        const float Ab = -phi * cs * ib + eta1, Bb = phi * ib;
+        w0 += Aa * uax + Ba * ubx;
+        w1 += Aa * uay + Ba * uby;
+        w2 += Aa * uaz + Ba * ubz;
+        S.wx[b] += Ab * ubx + Bb * uax;
+        S.wy[b] += Ab * uby + Bb * uay;
+        S.wz[b] += Ab * ubz + Bb * uaz;
+      }
+      __syncwarp();
+    }
+    if (x < sc.nown) {
+      S.wx[sc.xb + x] += w0;
+      S.wy[sc.xb + x] += w1;
+      S.wz[sc.xb + x] += w2;
+    }
+    __syncwarp();
+  }
+}
+
 // Dispatch on the block's grid size: eta count 1..NEK, zeta chain length rounded up to 3, 5 or 6
 // (at most NZK).  Only instances within the kernel's bounds are linked, which keeps the
 // kernel's register allocation to what its potential needs.
@@ -1016,6 +1139,13 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, true);
       if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, true);
       __syncwarp();
+      if constexpr (GEN) {
+        if (A.fn) {
+          symm_block_fn(S, A, P.atab + A.tab, make_sched(J, K, j0, nJ, k0, nK), Gi);
+          __syncwarp();
+          continue;
+        }
+      }
       run_block<false, NEK, NZK, GEN>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
       for (int f = lane; f < A.n; f += 32) Gi[A.off + f] = A.norm * S.scratch[(int)P.atab[A.tab + f]];
@@ -1109,6 +1239,14 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
       }
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, false);
       if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, false);
+      if constexpr (GEN) {
+        if (A.fn) {
+          __syncwarp();
+          force_block_fn(S, A, P.atab + A.tab, make_sched(J, K, j0, nJ, k0, nK), gi);
+          __syncwarp();
+          continue;
+        }
+      }
       // dE/dG on the function grid, one lane per grid cell (duplicates of a cell add up in file order)
       for (int c = lane; c < NE_MAX * NL * NZ_MAX; c += 32) {
         float v = 0.f;

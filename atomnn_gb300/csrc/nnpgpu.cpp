@@ -1088,6 +1088,12 @@ extern "C" int nnpgpu_train_force_grad(nnpgpu_ctx* c, int nstruc, const int* nat
   if (loss < 0 || loss > 3) return set_error(c, NNPGPU_ERR_INVALID, "train_force: loss must be 0 (MSE), 1 (MAE), 2 (HUBER) or 3 (ASINH)");
   if ((loss >= 2) && !(delta > 0)) return set_error(c, NNPGPU_ERR_INVALID, "train_force: HUBER and ASINH need delta > 0");
   if (!(beta >= 0) || !std::isfinite(beta)) return set_error(c, NNPGPU_ERR_INVALID, "train_force: beta must be finite and >= 0");
+  for (int I = 0; I < c->pot.ntypes; ++I)
+    for (int q = 0; q < NB_MAX; ++q)
+      if (c->P.ang[I][q].n > 0 && c->P.ang[I][q].fn)
+        return set_error(c, NNPGPU_ERR_UNSUPPORTED,
+                         "train_force: angular blocks with a real zeta or more than 4 widths or 2 lambdas are not implemented in the "
+                         "force trainer's tangent pass (energies and forces support them)");
   size_t N = 0;
   for (int s = 0; s < nstruc; ++s) {
     if (!natoms || natoms[s] <= 0) return set_error(c, NNPGPU_ERR_INVALID, "train_force: every structure needs atoms");

@@ -264,8 +264,24 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
         if (std::find(ie.begin(), ie.end(), v) == ie.end()) ie.push_back(v);
         if (std::find(lams.begin(), lams.end(), b.lam[f]) == lams.end()) lams.push_back(b.lam[f]);
       }
-      if ((int)ie.size() > NE_MAX) unsup("more than " + std::to_string(NE_MAX) + " distinct angular widths per block");
-      if ((int)lams.size() > NL) unsup("more than two distinct lambda values per block");
+      // blocks whose functions leave the (width) x (lambda) x (zeta = 2^m) grid - real zeta, more
+      // than NE_MAX widths or NL lambdas - take the per-function path (a.fn) of the GEN kernels
+      bool fn = (int)ie.size() > NE_MAX || (int)lams.size() > NL;
+      for (int f = 0; f < n; ++f) {
+        bool pow2 = false;
+        for (int k = 0; k < NZ_MAX; ++k) pow2 = pow2 || b.zeta[f] == (double)(1 << k);
+        if (!pow2) fn = true;
+        if (!(b.zeta[f] >= 1.0) || !std::isfinite(b.zeta[f])) unsup("angular zeta below 1 or not finite");
+      }
+      if (fn) {
+        a.fn = 1;
+        a.ne = 1;
+        a.nl = 1;
+        a.nz = 1;
+        a.mom = 0;
+        P.gen = 1;
+        continue;
+      }
       a.ne = (int)ie.size();
       a.nl = (int)lams.size();
       for (int e = 0; e < a.ne; ++e) a.ietap[e] = (float)ie[e];
@@ -340,9 +356,21 @@ std::vector<float> build_ang_tables(const HPot& pot, PotParams& P) {
       if (a.n == 0) continue;
       while (tab.size() % 4) tab.push_back(0.f);
       a.tab = (int)tab.size();
+      const HBasisA& b = pot.ang[I][q];
+      if (a.fn) {
+        // per function: 1/eta^alpha (BasisA::init, basis_angular.cpp:168-173), lambda, zeta, 0
+        for (int f = 0; f < a.n; ++f) {
+          double ie = 1.0;
+          for (int k = 0; k < b.alpha; ++k) ie *= 1.0 / b.eta[f];
+          tab.push_back((float)ie);
+          tab.push_back((float)b.lam[f]);
+          tab.push_back((float)b.zeta[f]);
+          tab.push_back(0.f);
+        }
+        continue;
+      }
       for (int f = 0; f < a.n; ++f) tab.push_back((float)a.gidx[f]);
       if (!a.mom) continue;
-      const HBasisA& b = pot.ang[I][q];
       const int w = a.ne * (MOM_N + 1);
       const double norm = norm_value(b.norm, b.rc);
       for (int f = 0; f < a.n; ++f) {

@@ -12,6 +12,9 @@
 //     skin/2 (same cell and species) re-decides the exact rc list from it instead of searching
 //     all atoms (neighbour mode 3).  Resident lists are evicted least-recently-used when they
 //     would exceed their share of the budget.  Requests of one key are processed in order.
+//   * a keyed request whose positions, species and cell equal (bit for bit) those of the key's
+//     last evaluated request is answered at submission from the key's resident results: its
+//     descriptors, network outputs and forces would be the same.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -49,6 +52,11 @@ struct Resident {
   size_t bytes = 0;
   bool busy = false;
   long long last = 0;
+  // the last evaluated request of this key (host copies): inputs and results
+  bool has_result = false;
+  std::vector<double> res_posn, res_cell, res_force;
+  std::vector<int> res_species;
+  double res_energy = 0;
 };
 }  // namespace
 
@@ -259,7 +267,18 @@ struct Serving::Impl {
           }
           off += 3 * (size_t)q->natoms;
           q->latency = std::chrono::duration<double>(now - q->t0).count();
-          if (q->key >= 0) res[q->key].busy = false;
+          if (q->key >= 0) {
+            Resident& r = res[q->key];
+            r.busy = false;
+            if (rcode == NNPGPU_OK) {
+              r.has_result = true;
+              r.res_posn = q->posn;
+              r.res_cell = q->cell;
+              r.res_species = q->species;
+              r.res_energy = q->energy;
+              r.res_force = q->force;
+            }
+          }
         }
       }
       cv.notify_all();
@@ -313,6 +332,18 @@ int Serving::submit(int natoms, const double* posn, const int* species, const do
     std::lock_guard<std::mutex> l(I.mu);
     q->id = I.next_id++;
     *id = q->id;
+    auto it = key >= 0 ? I.res.find(key) : I.res.end();
+    if (it != I.res.end() && it->second.has_result && it->second.res_posn == q->posn && it->second.res_species == q->species &&
+        it->second.res_cell == q->cell) {
+      // unchanged inputs: the key's resident results are this request's results
+      q->energy = it->second.res_energy;
+      q->force = it->second.res_force;
+      q->status = NNPGPU_OK;
+      q->latency = std::chrono::duration<double>(Clock::now() - q->t0).count();
+      it->second.last = ++I.tick;
+      I.reqs[q->id] = std::move(q);
+      return NNPGPU_OK;
+    }
     I.queue.push_back(q.get());
     I.reqs[q->id] = std::move(q);
   }

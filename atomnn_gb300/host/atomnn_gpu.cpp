@@ -429,20 +429,46 @@ void NeighborList::build(const Structure& struc, double rc) {
   build(tmp, struc, rc);
 }
 
-void NeighborList::build(const NNP& nnp, const Structure& struc, double rc) {
+void NeighborList::build(const NNP& nnp, const Structure& struc, double rc) { build_atoms(nnp, struc, rc, {}, true); }
+
+void NeighborList::build(const Structure& struc, double rc, int ii) {
+  if (ii < 0 || ii >= struc.nAtoms()) throw std::invalid_argument("NeighborList::build: atom index out of range");
+  std::vector<int> one(1, ii);
+  build(struc, rc, one);
+}
+
+void NeighborList::build(const Structure& struc, double rc, const std::vector<int>& subset) {
+  std::shared_ptr<nnpgpu_ctx> c;
+  {
+    std::lock_guard<std::mutex> l(g_last_mu);
+    c = g_last.lock();
+  }
+  if (!c) throw std::runtime_error("NeighborList::build: read a potential (NNP::read) first; it provides the GPU context");
+  for (int ii : subset)
+    if (ii < 0 || ii >= struc.nAtoms()) throw std::invalid_argument("NeighborList::build: atom index out of range");
+  NNP tmp;
+  tmp.ctx_ = c;
+  build_atoms(tmp, struc, rc, subset, false);
+}
+
+void NeighborList::build_atoms(const NNP& nnp, const Structure& struc, double rc, const std::vector<int>& subset, bool all) {
   if (!nnp.ctx()) throw std::runtime_error("NeighborList::build: no potential read");
   if (!(rc > 0)) throw std::invalid_argument("NeighborList::build: invalid cutoff");
   const int n = struc.nAtoms();
   std::vector<double> posn(3 * (size_t)std::max(n, 1));
   for (int i = 0; i < n; ++i)
     for (int x = 0; x < 3; ++x) posn[3 * (size_t)i + x] = struc.posn(i)[x];
+  const std::array<double, 9>& R = struc.R();  // column-major, columns = lattice vectors
+  double fro = 0.0;
+  for (double v : R) fro += v * v;
+  const bool periodic = fro > 0.0;
   std::vector<int> count(std::max(n, 1));
   int cap = 64;
   for (;;) {
     std::vector<int> index((size_t)std::max(n, 1) * cap), shift((size_t)std::max(n, 1) * cap * 3);
     std::vector<float> r((size_t)std::max(n, 1) * cap * 4);
     std::vector<unsigned char> mn((size_t)std::max(n, 1) * cap);
-    const int code = nnpgpu_neighbors_rc(nnp.ctx(), rc, n, posn.data(), struc.R().data(), cap, count.data(), index.data(), r.data(),
+    const int code = nnpgpu_neighbors_rc(nnp.ctx(), rc, n, posn.data(), R.data(), cap, count.data(), index.data(), r.data(),
                                          mn.data(), shift.data());
     if (code == NNPGPU_ERR_CAPACITY && cap < 1024) {
       int need = cap;
@@ -452,19 +478,30 @@ void NeighborList::build(const NNP& nnp, const Structure& struc, double rc) {
     }
     check(nnp.ctx(), code, "NeighborList::build");
     rc_ = rc;
-    neigh_.assign(n, {});
-    for (int i = 0; i < n; ++i) {
+    if (all) neigh_.assign(n, {});
+    else neigh_.resize(n);
+    auto fill = [&](int i) {
       neigh_[i].resize(count[i]);
       for (int s = 0; s < count[i]; ++s) {
         const size_t g = (size_t)i * cap + s;
         Neighbor& nb = neigh_[i][s];
-        nb.index() = index[g];
-        nb.r() = Vec3d(r[4 * g], r[4 * g + 1], r[4 * g + 2]);
-        nb.dr() = r[4 * g + 3];
+        const int j = index[g];
+        const int T[3] = {shift[3 * g], shift[3 * g + 1], shift[3 * g + 2]};
+        // r = posn(i) - posn(j) - R T in FP64 (the reference's rIJ - R_n, src/struc/neighbor.cpp:106-110)
+        Vec3d v;
+        for (int x = 0; x < 3; ++x) v[x] = struc.posn(i)[x] - struc.posn(j)[x] - (R[x] * T[0] + R[3 + x] * T[1] + R[6 + x] * T[2]);
+        nb.r() = v;
+        nb.dr() = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        nb.index() = (periodic && (int)struc.index().size() == n) ? struc.index(j) : j;
+        nb.type() = ((int)struc.type().size() == n) ? struc.type(j) : -1;
         nb.min() = mn[g] != 0;
-        nb.cell() = {shift[3 * g], shift[3 * g + 1], shift[3 * g + 2]};
+        nb.cell() = {T[0], T[1], T[2]};
       }
-    }
+    };
+    if (all)
+      for (int i = 0; i < n; ++i) fill(i);
+    else
+      for (int i : subset) fill(i);
     return;
   }
 }

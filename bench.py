@@ -8,8 +8,15 @@ rule and force gather, all on the GPU.  ``value`` is atoms/s with inputs residen
 ``e2e`` is the same through the host-buffer C API (copies inside the timed region).
 
 ``--impl reference`` times the reference algorithm on the host CPU cores instead: the FP64 C++
-restatement in oracle/ (the reference itself cannot be built here: Eigen and MPI are absent),
-over all host cores, on bounded samples of the same workload.
+restatement in oracle/, which reproduces the reference's own code bit for bit on the pinned
+fixtures (the reference's sources are not on this machine), over all host cores: each step is
+one of eight size strata of the workload (every eighth structure by size, largest first), so
+eight steps cover it once.
+
+Besides the headline, the line carries per-configuration figures (``configs``) for the 64-atom
+one-species cell, the 1728-atom two-species cell and the 65,536-atom cell with its 96-128-128-1
+networks: GPU atoms/s of the plain FP32 and the batched BF16 path, the oracle's single-thread
+atoms/s, and the energy and force errors against FP64.
 """
 import argparse
 import json
@@ -50,14 +57,18 @@ def _oracle_eval(args):
     return e, F
 
 
-def cpu_sample(strucs, target_atoms, offset=0):
-    out, tot, k = [], 0, offset
-    while tot < target_atoms:
-        s = strucs[k % len(strucs)]
-        out.append(s)
-        tot += s.natoms
-        k += 1
-    return out, tot
+NSTRATA = 8
+
+
+def strata(strucs, n=NSTRATA):
+    """The workload's structures sorted by size (largest first) and dealt into n strata: every
+    stratum holds every n-th structure by size rank, so each has the workload's size mix."""
+    order = sorted(range(len(strucs)), key=lambda k: -strucs[k].natoms)
+    return [[strucs[k] for k in order[q::n]] for q in range(n)]
+
+
+def largest_first(strucs):
+    return sorted(strucs, key=lambda s: -s.natoms)
 
 
 class OraclePool:
@@ -71,6 +82,8 @@ class OraclePool:
         self.pool.map(_oracle_eval, [(np.zeros((1, 3)), np.zeros(1, np.int32), np.eye(3) * 20.0)] * procs)
 
     def run(self, strucs):
+        """E+F of every structure, one task per structure in the given order (largest first
+        balances the processes); returns (seconds, results)."""
         t0 = time.perf_counter()
         res = self.pool.map(_oracle_eval, [(s.posn, s.species, s.cell) for s in strucs], chunksize=1)
         return time.perf_counter() - t0, res
@@ -167,33 +180,134 @@ def peaks():
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
-    pot = W.make_potential(WORKLOAD)
     potpath = W.workload_files(WORKLOAD, WORK_DIR)
     strucs = W.make_structures(WORKLOAD)
     procs = os.cpu_count() or 1
     pool = OraclePool(potpath, procs)
-    per_step_atoms = int(args.ref_step_atoms or 600 * procs)
+    parts = strata(strucs)
     times, atoms = [], []
-    off = 0
     for k in range(args.warmup + args.steps):
-        sample, tot = cpu_sample(strucs, per_step_atoms, off)
-        off += len(sample)
+        sample = parts[k % NSTRATA]
         dt, _ = pool.run(sample)
         if k >= args.warmup:
             times.append(dt)
-            atoms.append(tot)
+            atoms.append(sum(s.natoms for s in sample))
     pool.close()
     value = sum(atoms) / sum(times)
+    sample_desc = ("each step: one of %d size strata of the 512-structure workload (every %d-th structure by size, %d structures, "
+                   "about %d atoms), largest first, one process per core; %d consecutive steps cover the workload once"
+                   % (NSTRATA, NSTRATA, len(parts[0]), sum(s.natoms for s in parts[0]), NSTRATA))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": {"workload": "%s: %s" % (WORKLOAD, "512 triclinic A/B structures, 16-2048 atoms, 56-64-64-1 networks"),
                        "parallelism": "host cores (process pool)"},
-            "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": procs, "kind": "port",
-                             "sample": "each step: consecutive structures of the workload totalling >= %d atoms" % per_step_atoms},
+            "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": procs, "kind": "port", "sample": sample_desc},
             "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+# ----------------------------------------------------------------------------- per-configuration lines
+CONFIGS = (
+    ("c1_small64", "small64", "64-atom one-species cubic cell (8.1 A), 16 G2 + 16 G4, 32-32-32-1 networks, rc 6.0 A"),
+    ("c2_cell1728", "cell1728", "1728-atom A:B 1:2 cubic cell at 0.07/A^3, 24 G2 + 32 G4 per species, 56-64-64-1 networks, rc 6.5 A"),
+    ("c4_cell65536", "cell65536", "65,536-atom A:B 1:2 cubic cell at 0.07/A^3, 32 G2 + 64 G4 per species, 96-128-128-1 networks, rc 6.5 A"),
+)
+
+
+def cpu_config_baselines(run_cpu):
+    """The oracle's single-thread E+F atoms/s per configuration (run before any GPU call).  The
+    65,536-atom cell is timed on a sample of 256 centres, each with the reference's full scan
+    over all atoms for its neighbour list (NeighborList::build with a subset), its descriptors,
+    network and chain rule: the per-atom cost of the whole evaluation."""
+    from oracle import pyoracle
+    out = {}
+    for key, name, _ in CONFIGS:
+        if not run_cpu:
+            out[key] = None
+            continue
+        pot = W.workload_files(name, WORK_DIR)
+        orc = pyoracle.OracleNNP(pot)
+        s = W.make_structures(name)[0]
+        if name == "cell65536":
+            centres = np.random.default_rng(5).choice(s.natoms, 256, replace=False)
+            t0 = time.perf_counter()
+            orc.compute_centres(s.posn, s.species, s.cell, centres)
+            dt = time.perf_counter() - t0
+            out[key] = {"atoms_per_s": len(centres) / dt, "cores": 1, "seconds": dt,
+                        "sample": "256 centres of the cell, each scanning all 65,536 atoms (O(N) per centre as in the reference)"}
+        else:
+            reps = 20 if s.natoms < 500 else 1
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                e, F, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+            dt = (time.perf_counter() - t0) / reps
+            out[key] = {"atoms_per_s": s.natoms / dt, "cores": 1, "seconds": dt, "sample": "the whole structure",
+                        "energy": e, "force": F}
+    return out
+
+
+def gpu_config_lines(E, device, stream, cpu):
+    """GPU atoms/s of each configuration through nnpgpu_compute_device (inputs in HBM; CUDA events
+    around 10 calls after 3 warm-up calls): the plain FP32 path (the batched flag off) and the
+    batched BF16 path, with their energy and force errors against FP64 (the oracle for the small
+    cells, the committed oracle fixture tests/golden/cell65536.npz for the large one)."""
+    import hashlib
+    import torch
+    out = {}
+    for key, name, desc in CONFIGS:
+        pot = W.workload_files(name, WORK_DIR)
+        s = W.make_structures(name)[0]
+        eng = E.Engine(pot, device=device)
+        try:
+            natoms = np.array([s.natoms], dtype=np.int32)
+            cells = s.cell_colmajor()
+            d_posn = torch.from_numpy(np.ascontiguousarray(s.posn)).to(device)
+            d_spec = torch.from_numpy(np.ascontiguousarray(s.species, dtype=np.int32)).to(device)
+            d_e = torch.zeros(1, dtype=torch.float64, device=device)
+            d_f = torch.zeros((s.natoms, 3), dtype=torch.float64, device=device)
+            line = {"workload": desc, "atoms": s.natoms}
+            for tag, flags in (("gpu_plain_fp32", E.ENERGY | E.FORCE), ("gpu_batched_bf16", E.ENERGY | E.FORCE | E.BATCHED | E.BF16)):
+                step = lambda: eng.compute_device(natoms, d_posn.data_ptr(), d_spec.data_ptr(), cells, flags, d_e.data_ptr(), d_f.data_ptr(),
+                                                  0, stream.cuda_stream)
+                for _ in range(3):
+                    step()
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                for _ in range(10):
+                    step()
+                b.record(stream)
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b) / 10
+                e = float(d_e.cpu()[0])
+                F = d_f.cpu().numpy()
+                err = None
+                if name == "cell65536":
+                    fx = os.path.join(REPO, "tests", "golden", "cell65536.npz")
+                    if os.path.exists(fx):
+                        g = np.load(fx)
+                        h = hashlib.sha256()
+                        for arr in (np.ascontiguousarray(s.posn, dtype=np.float64), np.ascontiguousarray(s.species, dtype=np.int32),
+                                    np.ascontiguousarray(s.cell, dtype=np.float64)):
+                            h.update(arr.tobytes())
+                        if h.hexdigest() == str(g["structure_sha256"][0]):
+                            dF = F[g["force_atoms"]] - g["force"]
+                            err = {"energy_err_per_atom": abs(e - float(g["energy"][0])) / s.natoms,
+                                   "force_rmse": float(np.sqrt((dF ** 2).mean())), "force_err_max": float(np.abs(dF).max()),
+                                   "against": "FP64 oracle fixture (every 8th atom's force)"}
+                elif cpu.get(key):
+                    dF = F - cpu[key]["force"]
+                    err = {"energy_err_per_atom": abs(e - cpu[key]["energy"]) / s.natoms, "force_rmse": float(np.sqrt((dF ** 2).mean())),
+                           "force_err_max": float(np.abs(dF).max()), "against": "FP64 oracle"}
+                line[tag] = {"atoms_per_s": s.natoms / (ms / 1000.0), "ms": ms, "errors": err}
+            if cpu.get(key):
+                line["cpu_oracle"] = {k: v for k, v in cpu[key].items() if k not in ("energy", "force")}
+            out[key] = line
+        finally:
+            eng.close()
+    return out
 
 
 # ----------------------------------------------------------------------------- native arm
@@ -204,14 +318,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--plain-steps", type=int, default=3)
-    ap.add_argument("--cpu-atoms-per-core", type=int, default=4000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-step-atoms", type=int, default=0)
+    ap.add_argument("--no-configs", action="store_true", help="skip the per-configuration lines")
     ap.add_argument("--count", type=int, default=512, help="structures of the workload (512 = the full workload)")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
-    ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--serve-seconds", type=float, default=60.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_info()
@@ -224,17 +337,33 @@ def main():
     natoms = np.array([s.natoms for s in strucs], dtype=np.int32)
     total_atoms = int(natoms.sum())
 
-    # CPU baseline first: the spawn pool starts before any GPU call
+    # CPU baselines first: the spawn pool starts before any GPU call.  All cores: one full pass
+    # over the workload's structures, largest first; one core: one size stratum of a 64-way split.
     cpu = None
+    cpu_cfg = {}
     if rank == 0 and not args.no_cpu_baseline:
         procs = os.cpu_count() or 1
         pool = OraclePool(potpath, procs)
-        sample, tot = cpu_sample(strucs, args.cpu_atoms_per_core * procs)
+        sample = largest_first(strucs)
+        tot = sum(x.natoms for x in sample)
         dt, res = pool.run(sample)
         pool.close()
+        one = strata(strucs, 64)[0]
+        from oracle import pyoracle
+        orc1 = pyoracle.OracleNNP(potpath)
+        t0 = time.perf_counter()
+        for x in one:
+            orc1.compute(x.posn, x.species, x.cell, force=True)
+        dt1 = time.perf_counter() - t0
         cpu = dict(value=tot / dt, unit="atoms/s", cores=procs, kind="port",
-                   sample="first %d structures of the workload (%d atoms), E+F, FP64 oracle, one process per core" % (len(sample), tot),
+                   sample="all %d structures of the workload (%d atoms) once, largest first, E+F, FP64 oracle, one process per core"
+                          % (len(sample), tot),
+                   single_thread={"value": sum(x.natoms for x in one) / dt1, "unit": "atoms/s", "cores": 1,
+                                  "sample": "every 64th structure by size (%d structures, %d atoms), E+F, one process"
+                                            % (len(one), sum(x.natoms for x in one))},
                    sample_structs=sample, sample_results=res, seconds=dt)
+    if rank == 0 and not args.no_configs:
+        cpu_cfg = cpu_config_baselines(not args.no_cpu_baseline)
 
     import torch
     torch.cuda.set_device(local)
@@ -343,12 +472,34 @@ def main():
         st = SV.run_stream(eng, pool, rate=args.serve_rate, duration=args.serve_seconds, seed=2)
         bu = SV.run_stream(eng, pool, rate=2000.0, duration=1.0, burst=True, repeat_frac=0.0, seed=3)
         eng.serve_stop()
+        # the plain FP32 path (one structure per call, inputs in HBM) on the same size mix: every
+        # structure of the request pool once
+        p_nat = np.array([x.natoms for x in pool], dtype=np.int32)
+        p_pos = torch.from_numpy(np.concatenate([x.posn for x in pool])).to(dev)
+        p_spe = torch.from_numpy(np.concatenate([x.species for x in pool]).astype(np.int32)).to(dev)
+        p_cel = np.concatenate([x.cell_colmajor() for x in pool])
+        p_e = torch.zeros(len(pool), dtype=torch.float64, device=dev)
+        p_f = torch.zeros((int(p_nat.sum()), 3), dtype=torch.float64, device=dev)
+        pstep = lambda: eng.compute_device(p_nat, p_pos.data_ptr(), p_spe.data_ptr(), p_cel, E.ENERGY | E.FORCE, p_e.data_ptr(),
+                                           p_f.data_ptr(), 0, sptr)
+        pstep()
+        torch.cuda.synchronize()
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pa.record(stream)
+        for _ in range(2):
+            pstep()
+        pb.record(stream)
+        torch.cuda.synchronize()
+        plain_serve = 2 * int(p_nat.sum()) / (pa.elapsed_time(pb) / 1000.0)
         pct = lambda a, q: float(np.percentile(a, q) * 1000.0) if len(a) else None
         serve_out = {
             "offered_req_per_s": args.serve_rate, "seconds": args.serve_seconds, "requests": st["requests"], "repeat_steps": st["repeats"],
             "p50_ms": pct(st["latencies"], 50), "p99_ms": pct(st["latencies"], 99), "atoms_per_s": st["atoms"] / st["wall"],
             "saturated": {"requests": bu["requests"], "atoms_per_s": bu["atoms"] / bu["wall"], "p50_ms": pct(bu["latencies"], 50),
                           "p99_ms": pct(bu["latencies"], 99)},
+            "plain_same_mix": {"atoms_per_s": plain_serve, "desc": "plain FP32 path, one structure per call, on the request pool's "
+                                                                   "%d structures (16-4096 atoms)" % len(pool)},
+            "saturated_vs_plain_same_mix": (bu["atoms"] / bu["wall"]) / plain_serve,
             "desc": "nnpgpu_serve_*: 3 slots, continuous batching, 40 GB admission budget, 1.0 A skin for resident keys, "
                     "sizes log-uniform 16-4096 atoms",
         }
@@ -363,11 +514,13 @@ def main():
         if min(stage.values()) <= 0:
             raise RuntimeError("stage tracing returned no timings: %r" % prof)
         t_desc = (stage["descriptors"] + stage["chain_rule"]) / 1000.0
-        fp32_peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        fp32_peak = sms * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
         ach = work["desc_flops"] / t_desc / 1e12
         roof = {"bound": "fp32", "kernel": "symm_kernel + force_kernel (descriptor and chain-rule triplet passes)",
                 "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak, "traffic": None,
-                "peak_source": "derived: 152 SMs x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json (no FP32 figure is measured)",
+                "peak_source": "derived: %d SMs (from the device) x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
+                               "(no FP32 figure is measured)" % sms,
                 "work": "convention flops P*(30+13 nR) + T*(60+25 nA) = %.4g per step" % work["desc_flops"],
                 "kernel_ms": t_desc * 1000.0}
         tfile = os.path.join(REPO, "profiles", "traffic.json")
@@ -415,12 +568,13 @@ def main():
                 "desc": "one structure at a time (12 launches per structure), FP32 networks"},
             "batched_fp32": {"value": total_atoms / (statistics.mean(fp32_ms) / 1000), "unit": "atoms/s", "ms_per_step": statistics.mean(fp32_ms)},
             "accuracy_vs_fp64_oracle": acc,
+            "accuracy_sample": None if cpu is None else "all %d structures of the workload" % len(cpu["sample_structs"]),
             "serving": serve_out,
         }
-        if serve_out is not None and out["plain"] is not None:
-            serve_out["saturated_vs_plain"] = serve_out["saturated"]["atoms_per_s"] / out["plain"]["value"]
         if cpu is not None:
-            out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread")}
+        if not args.no_configs:
+            out["configs"] = gpu_config_lines(E, dev, stream, cpu_cfg)
         print(json.dumps(out), flush=True)
     eng.close()
     if ws > 1:

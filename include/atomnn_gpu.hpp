@@ -162,11 +162,14 @@ class Structure {
 };
 
 // One entry of a neighbour list (Neighbor, src/struc/neighbor.hpp:28-54): r points from the
-// neighbour's image to the centre, cell is the image's integer lattice translation.
+// neighbour's image to the centre, dr is its length, type the neighbour's type (struc.type(j)),
+// cell the image's integer lattice translation.
 class Neighbor {
  public:
   int& index() { return index_; }
   const int& index() const { return index_; }
+  int& type() { return type_; }
+  const int& type() const { return type_; }
   Vec3d& r() { return r_; }
   const Vec3d& r() const { return r_; }
   double& dr() { return dr_; }
@@ -178,6 +181,7 @@ class Neighbor {
 
  private:
   int index_ = 0;
+  int type_ = -1;
   Vec3d r_;
   double dr_ = 0.0;
   bool min_ = false;
@@ -187,16 +191,33 @@ class Neighbor {
 class NNP;
 
 // Neighbour lists of one structure, built on the GPU (NeighborList::build,
-// src/struc/neighbor.cpp:59-171): same entries, order and minimum-image flags.  Vectors are
-// the engine's FP32 values widened to double.
+// src/struc/neighbor.cpp:59-171): same entries, order and minimum-image flags.  Vectors and
+// distances are FP64: r = posn(i) - posn(j) - R * cell, recomputed on the host from the image's
+// lattice translation.  Entries of a periodic structure carry struc.index(j) as their index (j
+// in a non-periodic one), as the reference's build does.
 class NeighborList {
  public:
   NeighborList() = default;
+  // NeighborList(const Structure&, double) (src/struc/neighbor.hpp:71): builds at once
+  NeighborList(const Structure& struc, double rc) { build(struc, rc); }
   // builds with the device context of the most recently read NNP (the reference's build has
   // no potential argument); throws std::runtime_error when no NNP has been read
   void build(const Structure& struc, double rc);
   void build(const NNP& nnp, const Structure& struc, double rc);
-  double rc() const { return rc_; }
+  // build(struc, rc, ii) and build(struc, rc, subset) (src/struc/neighbor.cpp:173-394): the list
+  // is resized to the structure's atoms and only atom ii's (the subset's) lists are rebuilt; the
+  // others keep their entries.  The overloads without rc use the list's last cutoff.
+  void build(const Structure& struc, double rc, int ii);
+  void build(const Structure& struc, double rc, const std::vector<int>& subset);
+  void build(const Structure& struc) { build(struc, rc_); }
+  void build(const Structure& struc, int ii) { build(struc, rc_, ii); }
+  void build(const Structure& struc, const std::vector<int>& subset) { build(struc, rc_, subset); }
+  void clear() {
+    rc_ = 0.0;
+    neigh_.clear();
+  }
+  double& rc() { return rc_; }
+  const double& rc() const { return rc_; }
   int size() const { return (int)neigh_.size(); }
   int size(int i) const { return (int)neigh_[i].size(); }
   std::vector<Neighbor>& neigh(int i) { return neigh_[i]; }
@@ -205,6 +226,8 @@ class NeighborList {
   const Neighbor& neigh(int i, int j) const { return neigh_[i][j]; }
 
  private:
+  // lists of the atoms in subset (every atom when all is set) into neigh_
+  void build_atoms(const NNP& nnp, const Structure& struc, double rc, const std::vector<int>& subset, bool all);
   double rc_ = 0.0;
   std::vector<std::vector<Neighbor>> neigh_;
 };

@@ -828,9 +828,13 @@ struct Nb {
   int T[3];
 };
 
-// NeighborList::build(const Structure&, double rc), src/struc/neighbor.cpp:59-171
-static void build_neighbors(const Cell& cell, int natoms, const V3* posn, double rc, std::vector<std::vector<Nb>>& out) {
+// NeighborList::build(const Structure&, double rc), src/struc/neighbor.cpp:59-171; with centres,
+// NeighborList::build(const Structure&, double rc, const std::vector<int>& subset)
+// (src/struc/neighbor.cpp:283-394): only the listed atoms' lists, each scanning every atom.
+static void build_neighbors(const Cell& cell, int natoms, const V3* posn, double rc, std::vector<std::vector<Nb>>& out,
+                            const std::vector<int>* centres = nullptr) {
   out.assign(natoms, {});
+  const int ncentre = centres ? (int)centres->size() : natoms;
   const double rc2 = rc * rc;
   if (cell.periodic) {
     // lattice vectors sorted from largest to smallest norm (std::sort on 3 elements is an
@@ -856,7 +860,8 @@ static void build_neighbors(const Cell& cell, int natoms, const V3* posn, double
     double fro = 0;
     for (int i = 0; i < 9; ++i) fro += cell.R[i] * cell.R[i];
     fro = std::sqrt(fro);
-    for (int i = 0; i < natoms; ++i) {
+    for (int ci = 0; ci < ncentre; ++ci) {
+      const int i = centres ? (*centres)[ci] : ci;
       for (int j = 0; j < natoms; ++j) {
         std::vector<Nb> nj;
         int D[3];
@@ -883,7 +888,8 @@ static void build_neighbors(const Cell& cell, int natoms, const V3* posn, double
       }
     }
   } else {
-    for (int i = 0; i < natoms; ++i)
+    for (int ci = 0; ci < ncentre; ++ci) {
+      const int i = centres ? (*centres)[ci] : ci;
       for (int j = 0; j < natoms; ++j) {
         const V3 t{posn[i][0] - posn[j][0], posn[i][1] - posn[j][1], posn[i][2] - posn[j][2]};
         const double d2 = sqn(t);
@@ -894,13 +900,17 @@ static void build_neighbors(const Cell& cell, int natoms, const V3* posn, double
           out[i].push_back(nb);
         }
       }
+    }
   }
 }
 
-// NNP::symm, src/nnp/nnp.cpp:334-381
-static void symm(NNP& nnp, int natoms, const int* type, const std::vector<std::vector<Nb>>& nl, std::vector<std::vector<double>>& G) {
+// NNP::symm, src/nnp/nnp.cpp:334-381 (with centres: those atoms only)
+static void symm(NNP& nnp, int natoms, const int* type, const std::vector<std::vector<Nb>>& nl, std::vector<std::vector<double>>& G,
+                 const std::vector<int>* centres = nullptr) {
   G.assign(natoms, {});
-  for (int i = 0; i < natoms; ++i) {
+  const int ncentre = centres ? (int)centres->size() : natoms;
+  for (int ci = 0; ci < ncentre; ++ci) {
+    const int i = centres ? (*centres)[ci] : ci;
     const NNH& h = nnp.nnh[type[i]];
     G[i].assign(h.nInput, 0.0);
     const std::vector<Nb>& L = nl[i];
@@ -927,10 +937,12 @@ static void symm(NNP& nnp, int natoms, const int* type, const std::vector<std::v
 // NNP::force (src/nnp/nnp.cpp:416-482) and NNP::compute (src/nnp/nnp.cpp:496-566):
 // both run one fpbp per atom then the same chain rule; compute also sums the network outputs.
 static double force(NNP& nnp, int natoms, const int* type, const std::vector<std::vector<Nb>>& nl,
-                    const std::vector<std::vector<double>>& G, std::vector<V3>& F) {
+                    const std::vector<std::vector<double>>& G, std::vector<V3>& F, const std::vector<int>* centres = nullptr) {
   F.assign(natoms, V3{0, 0, 0});
   double energy = 0;
-  for (int i = 0; i < natoms; ++i) {
+  const int ncentre = centres ? (int)centres->size() : natoms;
+  for (int ci = 0; ci < ncentre; ++ci) {
+    const int i = centres ? (*centres)[ci] : ci;
     const NNH& h = nnp.nnh[type[i]];
     std::vector<double> dEdG(h.nInput);
     energy += h.nn.fpbp(G[i].data(), dEdG.data());
@@ -1130,6 +1142,38 @@ extern "C" int oracle_compute(void* nnpv, int natoms, const double* posn, const 
       if (force_out)
         for (int i = 0; i < natoms; ++i) for (int x = 0; x < 3; ++x) force_out[3 * i + x] = F[i][x];
     }
+    if (energy) *energy = e;
+    return 0;
+  } catch (...) {
+    return -2;
+  }
+}
+
+// The per-centre work of oracle_compute (E+F) for a subset of centre atoms: their neighbour
+// lists (each scanning every atom, as NeighborList::build(struc, rc, subset) does), descriptors,
+// network passes and chain rule.  Returns the centres' network outputs plus vacuum energies in
+// *energy.  The cost per centre equals that of the full evaluation, so a sample of centres times
+// the full structure's per-atom cost.
+extern "C" int oracle_compute_centres(void* nnpv, int natoms, const double* posn, const int* type, const double* cellp, int ncentre,
+                                      const int* centres, double* energy) {
+  try {
+    NNP& nnp = *(NNP*)nnpv;
+    for (int i = 0; i < natoms; ++i)
+      if (type[i] < 0 || type[i] >= nnp.ntypes) return -3;
+    std::vector<int> sub(centres, centres + ncentre);
+    for (int i : sub)
+      if (i < 0 || i >= natoms) return -3;
+    Cell cell;
+    cell.init(cellp);
+    std::vector<V3> p(natoms);
+    for (int i = 0; i < natoms; ++i) p[i] = V3{posn[3 * i], posn[3 * i + 1], posn[3 * i + 2]};
+    std::vector<std::vector<Nb>> nl;
+    build_neighbors(cell, natoms, p.data(), nnp.rc, nl, &sub);
+    std::vector<std::vector<double>> G;
+    orc::symm(nnp, natoms, type, nl, G, &sub);
+    std::vector<V3> F;
+    double e = orc::force(nnp, natoms, type, nl, G, F, &sub);
+    for (int i : sub) e += nnp.nnh[type[i]].energy;
     if (energy) *energy = e;
     return 0;
   } catch (...) {

@@ -59,6 +59,10 @@ int oracle_compute(void* nnp, int natoms, const double* posn, const int* type, c
 /* Energy and dE/dG of one atomic network (ANN::fpbp + DODZ::grad, src/ml/nn.cpp:1215-1233,1620-1628).
  * Returns the network output (without vacuum energy). */
 double oracle_network(void* nnp, int type, const double* symm, double* dedg);
+// E+F work of a subset of centre atoms (lists scanning every atom, descriptors, networks, chain
+// rule), for timing samples of large structures; energy = the centres' network outputs + vacuum
+int oracle_compute_centres(void* nnp, int natoms, const double* posn, const int* type, const double* cell, int ncentre,
+                           const int* centres, double* energy);
 /* network parameters of a type (ANN::size) and the energy trainer's batch error and gradient */
 int oracle_nnp_nparams(const void* nnp, int type);
 int oracle_train_grad(void* nnp, int nstruc, const int* natoms, const double* symm, int stride, const int* type,

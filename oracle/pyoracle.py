@@ -40,6 +40,7 @@ def lib():
         L.oracle_neighbors.argtypes = [dp, ip, vp, vp, ip, vp, vp, vp, vp, vp, vp]
         L.oracle_compute.argtypes = [vp, ip, vp, vp, vp, ip, vp, vp, vp, ip]
         L.oracle_network.argtypes = [vp, ip, vp, vp]
+        L.oracle_compute_centres.argtypes = [vp, ip, vp, vp, vp, ip, vp, vp]
         L.oracle_network.restype = dp
         L.oracle_nnp_nparams.argtypes = [vp, ip]
         L.oracle_train_grad.argtypes = [vp, ip, vp, vp, ip, vp, vp, ip, dp, vp, vp]
@@ -96,6 +97,19 @@ class OracleNNP:
         if rc != 0:
             raise RuntimeError("oracle_compute failed (%d)" % rc)
         return float(e[0]), F, G
+
+    def compute_centres(self, posn, species, cell, centres):
+        """E+F work of the listed centre atoms only (timing samples of large cells); returns the
+        centres' atomic energies summed (vacuum energies included)."""
+        posn = np.ascontiguousarray(posn, dtype=np.float64)
+        species = np.ascontiguousarray(species, dtype=np.int32)
+        centres = np.ascontiguousarray(centres, dtype=np.int32)
+        cellc = None if cell is None else np.ascontiguousarray(np.asarray(cell, dtype=np.float64).T).ravel()
+        e = np.zeros(1)
+        rc = lib().oracle_compute_centres(self._h, posn.shape[0], _ptr(posn), _ptr(species), _ptr(cellc), len(centres), _ptr(centres), _ptr(e))
+        if rc != 0:
+            raise RuntimeError("oracle_compute_centres failed (%d)" % rc)
+        return float(e[0])
 
     def train_grad(self, structures, energy_ref, loss=0, delta=1.0):
         """The energy trainer's batch error and gradient (NNPTE::error, src/nnp/nnpte.cpp:870-921) on

@@ -6,7 +6,9 @@
 // prints: "nlist <atoms> <entries> <min entries>", "symm <i> <k> <value>" for atom 0,
 //         "energy <E>", "cached <E>" (the networks on descriptors written to and read back from
 //         a binary structure file), "positions <E>" (descriptors cleared: from the positions),
-//         "compute <E without vacuum>", "force <i> <fx> <fy> <fz>", "batched <E>"
+//         "compute <E without vacuum>", "force <i> <fx> <fy> <fz>", "batched <E>", "trainer <E>" and
+//         "tool <E> <f0x>" (the reference's trainer and compute-tool loops), "nbtype ok",
+//         "r64 <j> <min> <rx> <ry> <rz> <dr>" for atom 0's list, "subset ok"
 #include <cstdio>
 #include <exception>
 #include <vector>
@@ -54,6 +56,51 @@ int main(int argc, char** argv) {
     std::vector<Structure> batch = {struc, struc};
     NNP::compute(nnp, batch, true);
     std::printf("batched %.10f %.10f\n", batch[0].energy(), batch[1].energy());
+    // the trainer's loop (src/nnp/nnpte.cpp:1962-1977) and the compute tool's loop
+    // (src/nnp/nnpce.cpp:259-281), with their own names and calls
+    {
+      std::vector<Structure> strucs(1, struc);
+      for (int i = 0; i < (int)strucs.size(); ++i) NNP::init(nnp, strucs[i]);
+      for (int i = 0; i < (int)strucs.size(); ++i) {
+        NeighborList nlist(strucs[i], nnp.rc());
+        NNP::symm(nnp, strucs[i], nlist);
+      }
+      std::printf("trainer %.10f\n", NNP::energy(nnp, strucs[0]));
+      const bool force = true;
+      std::vector<double> energy_nnp(strucs.size(), 0.0);
+      for (int i = 0; i < (int)strucs.size(); ++i) {
+        NeighborList nlist;
+        nlist.build(strucs[i], nnp.rc());
+        NNP::symm(nnp, strucs[i], nlist);
+        NNP::energy(nnp, strucs[i]);
+        if (force) NNP::force(nnp, strucs[i], nlist);
+        energy_nnp[i] = strucs[i].energy();
+      }
+      std::printf("tool %.10f %.10f\n", energy_nnp[0], strucs[0].force(0)[0]);
+    }
+    // Neighbor::type, the FP64 vectors of atom 0, and the one-atom and subset builds
+    {
+      bool types = true;
+      for (int i = 0; i < nlist.size(); ++i)
+        for (int j = 0; j < nlist.size(i); ++j) types = types && nlist.neigh(i, j).type() == struc.type(nlist.neigh(i, j).index());
+      std::printf("nbtype %s\n", types ? "ok" : "bad");
+      for (int j = 0; j < nlist.size(0); ++j) {
+        const Neighbor& nb = nlist.neigh(0, j);
+        std::printf("r64 %d %d %.17g %.17g %.17g %.17g\n", nb.index(), nb.min() ? 1 : 0, nb.r()[0], nb.r()[1], nb.r()[2], nb.dr());
+      }
+      const int last = struc.nAtoms() - 1;
+      NeighborList one;
+      one.build(struc, nnp.rc(), last);
+      NeighborList sub;
+      sub.rc() = nnp.rc();
+      sub.build(struc, std::vector<int>{0, last});
+      bool same = one.size() == nlist.size() && one.size(0) == 0 && one.size(last) == nlist.size(last);
+      same = same && sub.size(0) == nlist.size(0) && sub.size(last) == nlist.size(last) && (last < 2 || sub.size(1) == 0);
+      for (int j = 0; same && j < nlist.size(last); ++j)
+        same = one.neigh(last, j).index() == nlist.neigh(last, j).index() && one.neigh(last, j).min() == nlist.neigh(last, j).min() &&
+               one.neigh(last, j).r()[0] == nlist.neigh(last, j).r()[0] && sub.neigh(last, j).dr() == nlist.neigh(last, j).dr();
+      std::printf("subset %s\n", same ? "ok" : "bad");
+    }
     // invalid input surfaces as the reference's exception type
     Structure bad = struc;
     bad.type(0) = 99;

@@ -49,22 +49,31 @@ def test_truncated_potential_is_io_error(native_lib, tmp_path):
     assert rc == engine.ERR_IO, msg
 
 
-def test_unsupported_forms_are_reported(native_lib, tmp_path):
-    """A zeta that is not a power of two is valid for the reference but not for the GPU kernels."""
-    from atomnn_gb300 import engine
+def _with_zeta(zeta):
     lines = open(os.path.join(GOLDEN, "small64.nnp")).read().splitlines()
     out, done = [], False
     for ln in lines:
         parts = ln.split()
         if not done and len(parts) == 3 and ln.startswith("\t") and parts[1] == "1.000000":
-            ln = "\t%s 3.000000 %s" % (parts[0], parts[2])
+            ln = "\t%s %s %s" % (parts[0], zeta, parts[2])
             done = True
         out.append(ln)
     assert done
-    p = tmp_path / "z3.nnp"
-    p.write_text("\n".join(out) + "\n")
+    return "\n".join(out) + "\n"
+
+
+def test_unsupported_forms_are_reported(native_lib, tmp_path):
+    """A real zeta is supported (per-function angular path); a zeta below 1 is refused with
+    NNPGPU_ERR_UNSUPPORTED, since the force term's cw^(zeta-1) diverges at cw = 0."""
+    from atomnn_gb300 import engine
+    p = tmp_path / "z05.nnp"
+    p.write_text(_with_zeta("0.500000"))
     rc, msg = _create(native_lib, str(p))
     assert rc == engine.ERR_UNSUPPORTED and "zeta" in msg
+    p = tmp_path / "z3.nnp"
+    p.write_text(_with_zeta("3.000000"))
+    rc, msg = _create(native_lib, str(p))
+    assert rc != engine.ERR_UNSUPPORTED, msg  # without a GPU the context fails later, with ERR_CUDA
 
 
 def test_no_gpu_fails_loudly(native_lib, pot_small64):

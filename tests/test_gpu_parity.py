@@ -415,3 +415,55 @@ def test_basis_families_against_oracle(native_lib, oracle_lib, tmp_path, kind, f
             off += s.natoms
     finally:
         eng.close()
+
+
+# ---------------------------------------------------------------- against the reference's own outputs
+_REF = np.load(os.path.join(GOLDEN, "reference.npz"))
+_REF_CASES = [str(c) for c in _REF["cases"]]
+
+
+@pytest.mark.parametrize("case", _REF_CASES)
+def test_against_reference_fixture(native_lib, tmp_path, case):
+    """The GPU path against outputs of the reference's own code (tests/golden/reference.npz, from
+    tests/golden/make_ref_golden.py): neighbour lists in the reference's order with its minimum
+    images (vectors to 2e-5 A), FP32 energies within 1e-5 eV/atom, symmetry functions within 1e-5
+    of the largest, forces within 1e-4 eV/A (scaled by the largest force over 2 eV/A for the
+    untrained option variants), and the BF16 path's force RMSE within 1e-3 eV/A."""
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import variants as V
+    from atomnn_gb300 import engine
+    eng = engine.Engine(V.write(str(_REF[case + "/variant"][0]), str(tmp_path)))
+    try:
+        strucs, prefixes = [], []
+        for k in range(int(_REF[case + "/nstruc"][0])):
+            p = "%s/%d/" % (case, k)
+            strucs.append(W.Structure(posn=_REF[p + "posn"], species=_REF[p + "species"], cell=_REF[p + "cell"]))
+            prefixes.append(p)
+        e, F, G = eng.compute(strucs, _flags("ENERGY", "FORCE", "SYMM", "BATCHED"))
+        ec, _, _ = eng.compute(strucs, _flags("ENERGY", "FORCE", "NO_VACUUM", "BATCHED"))
+        eb, Fb, _ = eng.compute(strucs, _flags("ENERGY", "FORCE", "BATCHED", "BF16"))
+        off = 0
+        for k, (s, p) in enumerate(zip(strucs, prefixes)):
+            Fr = _REF[p + "force"]
+            fscale = 1.0 if case in ("small64", "mixed3", "cluster20", "edge") else max(1.0, float(np.abs(Fr).max()) / 2.0)
+            n = max(s.natoms, 1)
+            assert abs(e[k] - _REF[p + "energy"][0]) / n <= E_TOL
+            assert abs(ec[k] - _REF[p + "energy_compute"][0]) / n <= E_TOL
+            if s.natoms:
+                assert np.abs(F[k] - Fr).max() <= F_TOL * fscale
+                assert np.sqrt(((Fb[k] - Fr) ** 2).mean()) <= 1e-3 * fscale
+            rows, Gr = _REF[p + "symm_atoms"], _REF[p + "symm"]
+            if len(rows):
+                Gs = G[off + rows, :Gr.shape[1]]
+                assert np.abs(Gs - Gr).max() <= G_TOL * max(np.abs(Gr).max(), 1.0)
+            off += s.natoms
+            if (p + "nb_count") in _REF.files and s.natoms:
+                g = eng.neighbors(s.posn, s.cell)
+                np.testing.assert_array_equal([len(x["index"]) for x in g], _REF[p + "nb_count"])
+                if len(_REF[p + "nb_index"]):
+                    np.testing.assert_array_equal(np.concatenate([x["index"] for x in g]), _REF[p + "nb_index"])
+                    np.testing.assert_array_equal(np.concatenate([x["min"] for x in g]).astype(np.uint8), _REF[p + "nb_min"])
+                    np.testing.assert_allclose(np.concatenate([x["r"] for x in g]), _REF[p + "nb_r"], rtol=0, atol=2e-5)
+    finally:
+        eng.close()

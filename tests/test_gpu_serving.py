@@ -56,6 +56,31 @@ def test_alone_equals_in_the_mix(served):
         assert abs(e - e_dir[k]) / ids[k][1].natoms <= E_TOL
         assert np.abs(F - F_dir[k]).max() <= F_TOL
         assert lat > 0
+    # served results against the FP64 oracle: the target and every fourth structure of the mix
+    # (BF16 networks: energy within 1e-3 eV/atom, force RMSE within 1e-3 eV/A)
+    from oracle import pyoracle
+    orc = pyoracle.OracleNNP(os.path.join(GOLDEN, "mixed512.nnp"))
+    for s, (e, F) in [(target, (e_mix, F_mix))] + [(ids[k][1], res[k][:2]) for k in range(0, len(ids), 4)]:
+        eo, Fo, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+        assert abs(e - eo) / s.natoms <= 1e-3
+        assert np.sqrt(((F - Fo) ** 2).mean()) <= 1e-3
+
+
+def test_unmoved_repeat_served_from_resident_results(served):
+    """A keyed request whose inputs equal the key's last evaluated ones is answered from the
+    resident results; a moved one is evaluated again."""
+    from atomnn_gb300 import engine
+    s = W.make_structures("mixed512", seed=66, count=1, sizes=[700])[0]
+    e1, F1, _ = _wait(served, served.submit(s, key=11), s.natoms)
+    e2, F2, _ = _wait(served, served.submit(s, key=11), s.natoms)
+    assert e2 == e1 and np.array_equal(F2, F1)
+    moved = W.Structure(posn=s.posn + 0.01, species=s.species, cell=s.cell)
+    e3, F3, _ = _wait(served, served.submit(moved, key=11), s.natoms)
+    e_ref, F_ref, _ = served.compute([moved], engine.ENERGY | engine.FORCE | engine.BATCHED | engine.BF16)
+    assert abs(e3 - e_ref[0]) / s.natoms <= E_TOL and np.abs(F3 - F_ref[0]).max() <= F_TOL
+    # a different key with the same inputs is not served from key 11's results, but agrees
+    e4, F4, _ = _wait(served, served.submit(s, key=12), s.natoms)
+    assert abs(e4 - e1) / s.natoms <= E_TOL and np.abs(F4 - F1).max() <= F_TOL
 
 
 def test_resident_md_steps_match_fresh_evaluation(served):

@@ -267,3 +267,15 @@ def test_cpp_api_matches_oracle(native_lib, tmp_path, oracle_lib):
     b = [r for r in rows if r[0] == "batched"][0]
     assert abs(float(b[1]) - eo) / s.natoms <= E_TOL and float(b[1]) == float(b[2])
     assert ["invalid_argument", "ok"] in rows
+    # the reference's trainer loop (NeighborList(struc, rc), NNP::symm, NNP::energy) and compute-tool
+    # loop (build, symm, energy, force) compiled unchanged against the surface
+    assert abs(float([r for r in rows if r[0] == "trainer"][0][1]) - eo) / s.natoms <= E_TOL
+    t = [r for r in rows if r[0] == "tool"][0]
+    assert abs(float(t[1]) - eo) / s.natoms <= E_TOL and abs(float(t[2]) - Fo[0, 0]) <= F_TOL
+    assert ["nbtype", "ok"] in rows and ["subset", "ok"] in rows
+    # FP64 neighbour vectors and distances of atom 0 (the reference keeps Eigen::Vector3d)
+    r64 = np.array([[float(x) for x in r[1:]] for r in rows if r[0] == "r64"])
+    np.testing.assert_array_equal(r64[:, 0].astype(int), nb[0]["index"])
+    np.testing.assert_array_equal(r64[:, 1].astype(bool), nb[0]["min"])
+    np.testing.assert_allclose(r64[:, 2:5], nb[0]["r"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(r64[:, 5], nb[0]["dr"], rtol=0, atol=1e-12)

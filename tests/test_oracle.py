@@ -269,3 +269,17 @@ def test_force_train_gradient_matches_finite_differences(oracle_lib, tmp_path, l
             fd = (vals[0] - vals[1]) / (2 * h)
             assert abs(fd - grad[off + q]) <= 1e-7 + 1e-5 * abs(fd), (t, q, fd, grad[off + q])
         off += p0.size
+
+
+def test_compute_centres_partitions_the_energy(oracle_lib, pot_mixed):
+    """oracle_compute_centres (the per-centre work used for CPU timing samples of large cells):
+    disjoint centre sets add up to the full evaluation's energy."""
+    orc = oracle_lib.OracleNNP(pot_mixed)
+    s = W.make_structures("mixed512", seed=12, count=1, sizes=[150])[0]
+    e, _, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+    half = np.arange(0, s.natoms, 2)
+    rest = np.arange(1, s.natoms, 2)
+    ea = orc.compute_centres(s.posn, s.species, s.cell, half)
+    eb = orc.compute_centres(s.posn, s.species, s.cell, rest)
+    assert abs(ea + eb - e) <= 1e-12 * max(1.0, abs(e))
+    assert abs(orc.compute_centres(s.posn, s.species, s.cell, np.arange(s.natoms)) - e) <= 1e-12 * max(1.0, abs(e))
