@@ -71,6 +71,11 @@ struct PotParams {
   // cutoff shared by every basis of centre type I (ccut 0: the bases differ)
   int ccut[NT_MAX];
   float crc[NT_MAX], cpirc[NT_MAX], crci[NT_MAX];
+  // shared moments of centre type I (msh 1): its moment blocks (at most three) share one pair
+  // weight and involve the mns <= 2 neighbour species msp[I][0..mns); mrep is one of the blocks
+  // (its widths and pair weight stand for all); the stored moments are [set][width][MOM_C]
+  int msh[NT_MAX], mns[NT_MAX], mrep[NT_MAX];
+  int msp[NT_MAX][2];
   RadialP rad[NT_MAX][NT_MAX];
   AngP ang[NT_MAX][NB_MAX];
 };

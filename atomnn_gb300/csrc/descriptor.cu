@@ -33,10 +33,12 @@ struct WarpSmem {
 // fit there: in the descriptor pass two sets of MOM_C per width plus the diagonal terms, in the
 // chain rule two contraction tables of MOM_Q float4 per width.  With kx, a second per-width
 // region holds the pair factors' derivative weights (IPOWP and SECHP blocks of the force pass).
-// ng floats at the end hold the centre's dE/dG row in the force pass (0 elsewhere).
+// ng floats at the end hold the centre's dE/dG row in the force pass (0 elsewhere).  scratch is 96
+// floats: the G4 grid sums, or a moment block's coefficients, or those of up to three blocks plus
+// the shared tables' degree-0 terms.
 __host__ __device__ inline int ex_stride(int cap) { return cap > MOM_EX ? cap : MOM_EX; }
 __host__ __device__ inline size_t warp_smem_floats(int cap, int ne, bool kx, int ng = 0) {
-  return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + (kx ? (size_t)ne * cap : 0) + 64 + 8 + ng;
+  return (size_t)12 * cap + (size_t)ne * ex_stride(cap) + (kx ? (size_t)ne * cap : 0) + 96 + 8 + ng;
 }
 
 __device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
@@ -49,8 +51,8 @@ __device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
   s.wx = w; s.wy = w + cap; s.wz = w + 2 * cap;
   s.orig = reinterpret_cast<int*>(w + 3 * cap);
   s.scratch = w + 4 * cap;
-  s.toff = reinterpret_cast<int*>(s.scratch + 64);
-  s.gi = s.scratch + 72;
+  s.toff = reinterpret_cast<int*>(s.scratch + 96);
+  s.gi = s.scratch + 104;
   return s;
 }
 
@@ -110,8 +112,8 @@ __device__ const signed char c_mom_up[MOM_Q][3] = {{1, 2, 3},    {4, 5, 6},    {
 // Moments of nsets slot ranges (set 0: [lo0,hi0), set 1: [lo1,hi1)) for every width of the block:
 // M[(set*ne + e)*MOM_C + r] = sum over the set's slots of w_e u^(a,b,c).  Each (set, width) pair
 // is summed by its own group of L lanes (L = 32 / pairs, rounded down to a power of two), so the
-// cross-lane reduction takes log2(L) shuffle levels instead of 5.  With Dg, set 0 also gives
-// Dg[e*(MOM_N+1) + n] = sum w_e^2 |u|^2n (the j == k terms of a J == K block).
+// cross-lane reduction takes log2(L) shuffle levels instead of 5.  With Dg, every set also gives
+// Dg[(set*ne + e)*(MOM_N+1) + n] = sum w_e^2 |u|^2n (the j == k terms of a J == K block).
 // GAUSS instances evaluate exp(-x) directly; the others go through ang_h.
 template <bool GAUSS>
 __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nsets, int lo0, int hi0, int lo1, int hi1,
@@ -124,7 +126,7 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nse
   const bool active = grp < pairs;
   const int set = active ? grp / A.ne : 0, e = active ? grp % A.ne : 0;
   const int lo = active ? (set ? lo1 : lo0) : 0, hi = active ? (set ? hi1 : hi0) : 0;
-  const bool want_dg = Dg && set == 0;
+  const bool want_dg = Dg != nullptr;
   float acc[MOM_C], dg[MOM_N + 1];
 #pragma unroll
   for (int r = 0; r < MOM_C; ++r) acc[r] = 0.f;
@@ -180,7 +182,7 @@ __device__ void build_moments(const WarpSmem& S, const AngP& A, bool cc, int nse
     for (int r = 0; r < MOM_C; ++r) M[(set * A.ne + e) * MOM_C + r] = acc[r];
     if (want_dg) {
 #pragma unroll
-      for (int n = 0; n <= MOM_N; ++n) Dg[e * (MOM_N + 1) + n] = dg[n];
+      for (int n = 0; n <= MOM_N; ++n) Dg[(set * A.ne + e) * (MOM_N + 1) + n] = dg[n];
     }
   }
 }
@@ -376,6 +378,135 @@ __device__ void force_mom_block(const WarpSmem& S, const AngP& A, const float* _
     if (!same) mom_contract<false>(S, A, cc, k0, k0 + nK, TJ, T0, b, false);
   }
   __syncwarp();
+}
+
+// ------------------------------------------------------------------ shared moments
+// Centre types whose moment blocks share one pair weight (PotParams::msh): the moments of each of
+// the (at most two) neighbour species are built once, and every moment block takes its inner
+// products from them; the chain rule contracts each neighbour once against the sum of the
+// tables of the blocks that contain its species.  The same sums as the per-block path.
+__device__ __forceinline__ int mom_set(const PotParams& P, int I, int sp) { return sp == P.msp[I][0] ? 0 : 1; }
+
+// G4 of every moment block of centre type I; gmom (may be null) receives the moments
+template <bool GEN>
+__device__ void symm_mom_shared(const WarpSmem& S, const PotParams& P, int I, bool cc, float* __restrict__ gmom, float* __restrict__ Gi) {
+  const int lane = threadIdx.x & 31;
+  const AngP& R = P.ang[I][P.mrep[I]];
+  const int ns = P.mns[I], ne = R.ne, nec = ne * MOM_C;
+  const int sp0 = P.msp[I][0], sp1 = ns > 1 ? P.msp[I][1] : sp0;
+  float* MS = S.ex;               // [set][e][MOM_C]
+  float* Dg = S.ex + ns * nec;    // [set][e][MOM_N+1]
+  const int lo0 = S.toff[sp0], hi0 = S.toff[sp0 + 1], lo1 = S.toff[sp1], hi1 = S.toff[sp1 + 1];
+  if (!GEN || R.phi == ANG_GAUSS) build_moments<true>(S, R, cc, ns, lo0, hi0, lo1, hi1, MS, Dg);
+  else if constexpr (GEN) build_moments<false>(S, R, cc, ns, lo0, hi0, lo1, hi1, MS, Dg);
+  __syncwarp();
+  if (gmom)
+    for (int t = lane; t < ns * nec; t += 32) gmom[t] = MS[t];
+  for (int J = 0; J < P.ntypes; ++J)
+    for (int K = J; K < P.ntypes; ++K) {
+      const AngP& A = P.ang[I][lidx(J, K)];
+      if (A.n == 0 || !A.mom) continue;
+      const int sJ = mom_set(P, I, J), sK = mom_set(P, I, K);
+      float* V = S.scratch;
+      if (lane < ne * (MOM_N + 1)) {
+        const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
+        const float* MJ = MS + sJ * nec + e * MOM_C;
+        const float* MK = MS + sK * nec + e * MOM_C;
+        float v = 0.f;
+        for (int r = mom_off(n); r < mom_off(n + 1); ++r) v = fmaf(c_mom_mult[r] * MJ[r], MK[r], v);
+        if (J == K) v = 0.5f * (v - Dg[(sJ * ne + e) * (MOM_N + 1) + n]);
+        V[lane] = v;
+      }
+      __syncwarp();
+      const int w = ne * (MOM_N + 1);
+      const float* __restrict__ M = P.atab + A.tab + A.n;
+      for (int f = lane; f < A.n; f += 32) {
+        float v = 0.f;
+        for (int k = 0; k < w; ++k) v = fmaf(M[f * w + k], V[k], v);
+        Gi[A.off + f] = v;
+      }
+      __syncwarp();
+    }
+}
+
+// chain rule of every moment block of centre type I from the stored moments gm
+template <bool GEN>
+__device__ void force_mom_shared(const WarpSmem& S, const PotParams& P, int I, bool cc, const float* __restrict__ gm,
+                                 const float* __restrict__ gi) {
+  const int lane = threadIdx.x & 31;
+  const AngP& R = P.ang[I][P.mrep[I]];
+  const int ns = P.mns[I], ne = R.ne, nec = ne * MOM_C, w = ne * (MOM_N + 1);
+  // coefficients b[blk][e][n] of each moment block (the coefficient matrix applied to dE/dG);
+  // the blocks' species pairs packed 4 bits each (J | K << 2) so that they stay in a register
+  int pk = 0, nb = 0;
+  for (int J = 0; J < P.ntypes; ++J)
+    for (int K = J; K < P.ntypes; ++K) {
+      const AngP& A = P.ang[I][lidx(J, K)];
+      if (A.n == 0 || !A.mom || nb >= 3) continue;
+      float* b = S.scratch + 20 * nb;
+      const float* __restrict__ M = P.atab + A.tab + A.n;
+      if (lane < w) {
+        float s0 = 0.f, s1 = 0.f;
+        int f = 0;
+        for (; f + 1 < A.n; f += 2) {
+          s0 = fmaf(gi[A.off + f], M[f * w + lane], s0);
+          s1 = fmaf(gi[A.off + f + 1], M[(f + 1) * w + lane], s1);
+        }
+        if (f < A.n) s0 = fmaf(gi[A.off + f], M[f * w + lane], s0);
+        b[lane] = s0 + s1;
+      }
+      pk |= (J | (K << 2)) << (4 * nb);
+      ++nb;
+    }
+  __syncwarp();
+  // tables of each species set: T_s[e][q] = sum over the blocks containing the species of
+  // b_(deg q + 1) times the other species' moments one degree up; T0_s[e] likewise with degree 0
+  float4* T = reinterpret_cast<float4*>(S.ex);
+  float* T0 = S.scratch + 60;  // [set][e]
+  if (lane < MOM_Q) {
+    const int u0 = c_mom_up[lane][0], u1 = c_mom_up[lane][1], u2 = c_mom_up[lane][2], dq = mom_deg(lane) + 1;
+    for (int se = 0; se < ns * ne; ++se) {
+      const int set = se / ne, e = se % ne;
+      const int spc = P.msp[I][set];
+      float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int k = 0; k < nb; ++k) {
+        const int bJ = (pk >> (4 * k)) & 3, bK = (pk >> (4 * k + 2)) & 3;
+        if (bJ != spc && bK != spc) continue;
+        const int other = bJ == spc ? bK : bJ;
+        const float bn = S.scratch[20 * k + e * (MOM_N + 1) + dq];
+        const float* Mg = gm + mom_set(P, I, other) * nec + e * MOM_C;
+        t.x = fmaf(bn, Mg[u0], t.x);
+        t.y = fmaf(bn, Mg[u1], t.y);
+        t.z = fmaf(bn, Mg[u2], t.z);
+      }
+      T[se * MOM_Q + lane] = t;
+    }
+  }
+  if (lane < ns * ne) {
+    const int set = lane / ne, e = lane % ne, spc = P.msp[I][set];
+    float t0 = 0.f;
+    for (int k = 0; k < nb; ++k) {
+      const int bJ = (pk >> (4 * k)) & 3, bK = (pk >> (4 * k + 2)) & 3;
+      if (bJ != spc && bK != spc) continue;
+      const int other = bJ == spc ? bK : bJ;
+      t0 = fmaf(S.scratch[20 * k + e * (MOM_N + 1)], gm[mom_set(P, I, other) * nec + e * MOM_C], t0);
+    }
+    T0[lane] = t0;
+  }
+  __syncwarp();
+  // each species' slots once; a species' own block (J == K) adds its diagonal term
+  for (int set = 0; set < ns; ++set) {
+    const int spc = P.msp[I][set];
+    int kd = -1;
+    for (int k = 0; k < nb; ++k)
+      if (((pk >> (4 * k)) & 3) == spc && ((pk >> (4 * k + 2)) & 3) == spc) kd = k;
+    const float* bd = kd >= 0 ? S.scratch + 20 * kd : S.scratch;
+    if (!GEN || R.phi == ANG_GAUSS)
+      mom_contract<true>(S, R, cc, S.toff[spc], S.toff[spc + 1], T + set * ne * MOM_Q, T0 + set * ne, bd, kd >= 0);
+    else if constexpr (GEN)
+      mom_contract<false>(S, R, cc, S.toff[spc], S.toff[spc + 1], T + set * ne * MOM_Q, T0 + set * ne, bd, kd >= 0);
+    __syncwarp();
+  }
 }
 
 // Stage the neighbour slots of atom i in shared memory, grouped by neighbour type.
@@ -1126,6 +1257,8 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
   }
 
   // ---- angular blocks (J <= K): G4
+  const bool msh = P.msh[I] != 0;
+  if (msh) symm_mom_shared<GEN>(S, P, I, cc, mom ? mom + (size_t)i * mstride : nullptr, Gi);
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
@@ -1133,6 +1266,7 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (A.mom) {
+        if (msh) continue;
         symm_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
         continue;
       }
@@ -1226,6 +1360,8 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
   __syncwarp();
 
   // ---- angular chain rule
+  const bool msh = P.msh[I] != 0;
+  if (msh) force_mom_shared<GEN>(S, P, I, cc, gm, gi);
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
@@ -1234,6 +1370,7 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
       if (A.mom) {
+        if (msh) continue;
         force_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, gm + A.moff, gi);
         continue;
       }

@@ -319,6 +319,37 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
       }
       ne_max = std::max(ne_max, a.ne);
     }
+    // moment blocks that share one pair weight (widths, alpha, cutoff, radius, family) and at
+    // most two neighbour species: the kernels build each species' moments once per centre and
+    // contract each neighbour once against the sum of its blocks' tables
+    {
+      std::vector<int> mq;
+      for (int q = 0; q < pot.ntypes * (pot.ntypes + 1) / 2; ++q)
+        if (P.ang[I][q].n > 0 && P.ang[I][q].mom) mq.push_back(q);
+      bool ok = mq.size() >= 2;
+      std::vector<int> sp;
+      for (size_t t = 0; ok && t < mq.size(); ++t) {
+        const AngP& a = P.ang[I][mq[t]];
+        const AngP& r = P.ang[I][mq[0]];
+        ok = a.ne == r.ne && a.alpha == r.alpha && a.cut == r.cut && a.rc == r.rc && a.phi == r.phi;
+        for (int e = 0; ok && e < a.ne; ++e) ok = a.ietap[e] == r.ietap[e];
+        for (int x = 0; x < pot.ntypes; ++x)
+          for (int y = x; y < pot.ntypes; ++y)
+            if (lidx(x, y) == mq[t]) {
+              if (std::find(sp.begin(), sp.end(), x) == sp.end()) sp.push_back(x);
+              if (std::find(sp.begin(), sp.end(), y) == sp.end()) sp.push_back(y);
+            }
+      }
+      ok = ok && sp.size() <= 2 && mq.size() <= 3;
+      if (ok) {
+        std::sort(sp.begin(), sp.end());
+        P.msh[I] = 1;
+        P.mns[I] = (int)sp.size();
+        P.mrep[I] = mq[0];
+        for (int t = 0; t < 2; ++t) P.msp[I][t] = t < (int)sp.size() ? sp[t] : -1;
+        moff = P.mns[I] * P.ang[I][mq[0]].ne * MOM_C;  // the shared moments replace the per-block ones
+      }
+    }
     P.mstride = std::max(P.mstride, (moff + 3) / 4 * 4);
     // one cutoff function and radius for every basis of this centre type: the kernels then
     // evaluate it once per neighbour
