@@ -638,28 +638,82 @@ __global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int ca
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
   const int n = min(nb_cnt[i], cap);
-  for (int s = lane; s < n; s += 32) {
-    const size_t src = (size_t)i * cap + s;
-    if (!code_min(nb_code[src])) continue;
-    const int j = nb_j[src];
-    if (pass == 0 ? (i > j) : (i < j || nb_rev[src] >= 0)) continue;
-    const int nj = min(nb_cnt[j], cap);
-    const int* L = nb_j + (size_t)j * cap;
-    int lo = 0, hi = nj;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (L[mid] < i) lo = mid + 1;
-      else hi = mid;
+  if (pass == 1) {
+    // what pass 0 left: a slot already paired is skipped on its reverse entry alone
+    for (int s = lane; s < n; s += 32) {
+      const size_t src = (size_t)i * cap + s;
+      if (nb_rev[src] >= 0 || !code_min(nb_code[src])) continue;
+      const int j = nb_j[src];
+      if (i < j) continue;
+      const int nj = min(nb_cnt[j], cap);
+      const int* L = nb_j + (size_t)j * cap;
+      int lo = 0, hi = nj;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (L[mid] < i) lo = mid + 1;
+        else hi = mid;
+      }
+      int found = -1;
+      for (int t = lo; t < nj && L[t] == i; ++t)
+        if (code_min(nb_code[(size_t)j * cap + t])) { found = t; break; }
+      if (found >= 0) {
+        nb_rev[(size_t)j * cap + found] = (int)src;
+      } else {
+        const int k = atomicAdd(&status[ST_ORPHANS], 1);
+        if (k < orphan_cap) orphans[k] = (int)src;
+      }
     }
-    int found = -1;
-    for (int t = lo; t < nj && L[t] == i; ++t)
-      if (code_min(nb_code[(size_t)j * cap + t])) { found = t; break; }
-    if (found >= 0) {
-      nb_rev[(size_t)j * cap + found] = (int)src;
-      if (pass == 0) nb_rev[src] = (int)((size_t)j * cap + found);
-    } else {
-      const int k = atomicAdd(&status[ST_ORPHANS], 1);
-      if (k < orphan_cap) orphans[k] = (int)src;
+    return;
+  }
+  // pass 0: RS slots per lane at a time, their binary searches advanced in lockstep so that the
+  // dependent loads of different searches overlap
+  constexpr int RS = 4;
+  for (int s0 = lane; s0 < n; s0 += 32 * RS) {
+    int tj[RS], lo[RS], hi[RS];
+#pragma unroll
+    for (int k = 0; k < RS; ++k) {
+      const int s = s0 + 32 * k;
+      tj[k] = -1;
+      lo[k] = 0;
+      hi[k] = 0;
+      if (s < n) {
+        const size_t src = (size_t)i * cap + s;
+        const int j = nb_j[src];
+        if (code_min(nb_code[src]) && i < j) {
+          tj[k] = j;
+          hi[k] = min(nb_cnt[j], cap);
+        }
+      }
+    }
+    bool more = true;
+    while (more) {
+      more = false;
+#pragma unroll
+      for (int k = 0; k < RS; ++k)
+        if (lo[k] < hi[k]) {
+          const int mid = (lo[k] + hi[k]) >> 1;
+          if (nb_j[(size_t)tj[k] * cap + mid] < i) lo[k] = mid + 1;
+          else hi[k] = mid;
+          more = more || lo[k] < hi[k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < RS; ++k) {
+      if (tj[k] < 0) continue;
+      const int j = tj[k];
+      const size_t src = (size_t)i * cap + s0 + 32 * k;
+      const int nj = min(nb_cnt[j], cap);
+      const int* L = nb_j + (size_t)j * cap;
+      int found = -1;
+      for (int t = lo[k]; t < nj && L[t] == i; ++t)
+        if (code_min(nb_code[(size_t)j * cap + t])) { found = t; break; }
+      if (found >= 0) {
+        nb_rev[(size_t)j * cap + found] = (int)src;
+        nb_rev[src] = (int)((size_t)j * cap + found);
+      } else {
+        const int o = atomicAdd(&status[ST_ORPHANS], 1);
+        if (o < orphan_cap) orphans[o] = (int)src;
+      }
     }
   }
 }
