@@ -251,13 +251,18 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
   // scaled inputs of this thread's atom -> split bf16 operand (zero rows past the tile end)
   {
     const int r = tid;
-    const float* g = (r < cnt) ? G + (size_t)perm[start + r] * gstride : nullptr;
+    // the row in 16-byte loads: rows are gstride floats (a multiple of 16) apart and the padded
+    // width k0p <= gstride, so whole float4 of the row are read
+    const float4* g4 = (r < cnt) ? reinterpret_cast<const float4*>(G + (size_t)perm[start + r] * gstride) : nullptr;
     for (int c0 = 0; c0 < net.k0p; c0 += 32) {
       float v[32];
 #pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        const int c = c0 + k;
-        v[k] = (g && c < net.nin) ? net.inpw[c] * (g[c] + net.inpb[c]) : 0.f;
+      for (int k4 = 0; k4 < 8; ++k4) {
+        const int c = c0 + 4 * k4;
+        const float4 x = (g4 && c < net.k0p) ? g4[c >> 2] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[4 * k4 + q] = (c + q < net.nin) ? net.inpw[c + q] * (xs[q] + net.inpb[c + q]) : 0.f;
       }
       store_row_split(a_hi, a_lo, r, c0, net.k0p, v, min(4, (net.k0p - c0) / 8));
     }
@@ -356,11 +361,19 @@ __global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constan
           for (int q = 0; q < 32; ++q) v[q] *= d[q];
           store_row_split(a_hi, a_lo, r, c0, n, v, 4);
         } else if (live) {
-          float* o = dEdG + (size_t)perm[start + r] * gstride;
+          // 16-byte stores; columns from nin up to the padded width k0p (<= gstride) get zeros
+          float4* o4 = reinterpret_cast<float4*>(dEdG + (size_t)perm[start + r] * gstride);
 #pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const int c = c0 + q;
-            if (c < net.nin) o[c] = v[q] * net.inpw[c];
+          for (int k4 = 0; k4 < 8; ++k4) {
+            const int c = c0 + 4 * k4;
+            if (c < net.k0p) {
+              float4 w;
+              w.x = (c < net.nin) ? v[4 * k4] * net.inpw[c] : 0.f;
+              w.y = (c + 1 < net.nin) ? v[4 * k4 + 1] * net.inpw[c + 1] : 0.f;
+              w.z = (c + 2 < net.nin) ? v[4 * k4 + 2] * net.inpw[c + 2] : 0.f;
+              w.w = (c + 3 < net.nin) ? v[4 * k4 + 3] * net.inpw[c + 3] : 0.f;
+              o4[c >> 2] = w;
+            }
           }
         }
       }

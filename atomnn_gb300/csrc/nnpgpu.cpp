@@ -658,6 +658,18 @@ extern "C" int nnpgpu_ninput(const nnpgpu_ctx* c, int type) {
   return c->pot.nin[type];
 }
 
+// True for page-locked host memory (cudaMallocHost, cudaHostRegister, a pinned torch tensor):
+// copies from and to it are DMA transfers that need no staging.
+static bool host_pinned(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
 static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* posn, const int* species, const double* cell,
                         int flags, double* energy, double* force, float* symm, bool device_io, cudaStream_t st,
                         const SkinRef* skins = nullptr) {
@@ -675,6 +687,10 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
     for (int a = 0; a < total; ++a)
       if (species[a] < 0 || species[a] >= c->pot.ntypes) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
   int cap = std::min(256, estimate_cap(c, nstruc, natoms, cell));  // the descriptor kernels take at most 256 slots
+  // page-locked caller buffers are read and written by DMA directly; others go through the
+  // context's pinned staging buffers
+  const bool direct_in = !device_io && total > 0 && host_pinned(posn) && host_pinned(species);
+  const bool direct_force = !device_io && (flags & NNPGPU_FORCE) && total > 0 && host_pinned(force);
   for (int attempt = 0; attempt < 4; ++attempt) {
     Uploaded U;
     int rc = prepare(c, nstruc, natoms, cell, cap, U, st, skins);
@@ -682,7 +698,12 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
     const size_t N = total;
     const double* dposn = posn;
     const int* dtype = species;
-    if (!device_io) {
+    if (direct_in) {
+      cudaMemcpyAsync(c->posn.p, posn, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(c->type.p, species, sizeof(int) * N, cudaMemcpyHostToDevice, st);
+      dposn = (const double*)c->posn.p;
+      dtype = (const int*)c->type.p;
+    } else if (!device_io) {
       // stage inputs through pinned memory
       const size_t in_bytes = sizeof(double) * 3 * N + sizeof(int) * N;
       if (!ensure_host(c, c->h_in, in_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
@@ -706,7 +727,9 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
       if (!ensure_host(c, c->h_out, out_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
       char* h = (char*)c->h_out.p;
       if (flags & NNPGPU_ENERGY) cudaMemcpyAsync(h, c->energy.p, sizeof(double) * nstruc, cudaMemcpyDeviceToHost, st);
-      if (flags & NNPGPU_FORCE) cudaMemcpyAsync(h + sizeof(double) * nstruc, c->force.p, sizeof(double) * 3 * N, cudaMemcpyDeviceToHost, st);
+      if (flags & NNPGPU_FORCE)
+        cudaMemcpyAsync(direct_force ? (void*)force : (void*)(h + sizeof(double) * nstruc), c->force.p, sizeof(double) * 3 * N,
+                        cudaMemcpyDeviceToHost, st);
       cudaMemcpyAsync(h + sizeof(double) * (nstruc + 3 * N), c->status.p, sizeof(int) * ST_WORDS, cudaMemcpyDeviceToHost, st);
       if (flags & NNPGPU_SYMM)
         cudaMemcpy2DAsync(symm, sizeof(float) * c->max_nin, c->G.p, sizeof(float) * c->gstride, sizeof(float) * c->max_nin, N,
@@ -718,7 +741,7 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
       if (need < 0) return need;
       if (need > 0) { cap = need; c->cap_hint = std::max(c->cap_hint, need); continue; }
       if (flags & NNPGPU_ENERGY) std::memcpy(energy, h, sizeof(double) * nstruc);
-      if (flags & NNPGPU_FORCE) std::memcpy(force, h + sizeof(double) * nstruc, sizeof(double) * 3 * N);
+      if ((flags & NNPGPU_FORCE) && !direct_force) std::memcpy(force, h + sizeof(double) * nstruc, sizeof(double) * 3 * N);
       accumulate_profile(c, flags);
       return NNPGPU_OK;
     }

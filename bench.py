@@ -10,8 +10,8 @@ rule and force gather, all on the GPU.  ``value`` is atoms/s with inputs residen
 ``--impl reference`` times the reference algorithm on the host CPU cores instead: the FP64 C++
 restatement in oracle/, which reproduces the reference's own code bit for bit on the pinned
 fixtures (the reference's sources are not on this machine), over all host cores: each step is
-one of eight size strata of the workload (every eighth structure by size, largest first), so
-eight steps cover it once.
+one of four size strata of the workload (every fourth structure by size, largest first), so
+four steps cover it once; the GPU arm's ``cpu_baseline`` times the same four strata.
 
 Besides the headline, the line carries per-configuration figures (``configs``) for the 64-atom
 one-species cell, the 1728-atom two-species cell and the 65,536-atom cell with its 96-128-128-1
@@ -57,7 +57,7 @@ def _oracle_eval(args):
     return e, F
 
 
-NSTRATA = 8
+NSTRATA = 4
 
 
 def strata(strucs, n=NSTRATA):
@@ -345,16 +345,21 @@ def main():
     natoms = np.array([s.natoms for s in strucs], dtype=np.int32)
     total_atoms = int(natoms.sum())
 
-    # CPU baselines first: the spawn pool starts before any GPU call.  All cores: one full pass
-    # over the workload's structures, largest first; one core: one size stratum of a 64-way split.
+    # CPU baselines first: the spawn pool starts before any GPU call.  All cores: the workload's
+    # four size strata (the reference arm's steps), each timed on its own, largest first; one
+    # core: one size stratum of a 64-way split.
     cpu = None
     cpu_cfg = {}
     if rank == 0 and not args.no_cpu_baseline:
         procs = os.cpu_count() or 1
         pool = OraclePool(potpath, procs)
-        sample = largest_first(strucs)
+        sample, res, dt = [], [], 0.0
+        for part in strata(strucs):
+            t_part, r_part = pool.run(part)
+            sample += part
+            res += r_part
+            dt += t_part
         tot = sum(x.natoms for x in sample)
-        dt, res = pool.run(sample)
         pool.close()
         one = strata(strucs, 64)[0]
         from oracle import pyoracle
@@ -364,8 +369,8 @@ def main():
             orc1.compute(x.posn, x.species, x.cell, force=True)
         dt1 = time.perf_counter() - t0
         cpu = dict(value=tot / dt, unit="atoms/s", cores=procs, kind="port",
-                   sample="all %d structures of the workload (%d atoms) once, largest first, E+F, FP64 oracle, one process per core"
-                          % (len(sample), tot),
+                   sample="all %d structures of the workload (%d atoms) once, as %d size strata timed one after the other "
+                          "(each largest first), E+F, FP64 oracle, one process per core" % (len(sample), tot, NSTRATA),
                    single_thread={"value": sum(x.natoms for x in one) / dt1, "unit": "atoms/s", "cores": 1,
                                   "sample": "every 64th structure by size (%d structures, %d atoms), E+F, one process"
                                             % (len(one), sum(x.natoms for x in one))},
@@ -459,18 +464,29 @@ def main():
     fp32_ms, _ = timed(batched, args.steps, 1) if bf16_ok else (ms, None)
     plain_ms, _ = timed(E.ENERGY | E.FORCE, args.plain_steps, 1) if args.plain_steps > 0 else (None, None)
 
-    # end to end through the host-buffer API (pinned staging, copies inside the timed region)
-    h_energy = np.zeros(len(strucs))
-    h_force = np.zeros((total_atoms, 3))
+    # end to end through the host-buffer API with page-locked host arrays (the library copies
+    # them by DMA, no staging), copies inside the timed region
+    keep = []
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.from_numpy(np.ascontiguousarray(a)).dtype, pin_memory=True)
+        keep.append(t)
+        v = t.numpy()
+        v[...] = a
+        return v
+
+    posn_h, species_h = pinned(posn), pinned(species)
+    h_energy = pinned(np.zeros(len(strucs)))
+    h_force = pinned(np.zeros((total_atoms, 3)))
     for _ in range(2):
-        eng.compute_flat(natoms, posn, species, cells, head_flags, h_energy, h_force)
+        eng.compute_flat(natoms, posn_h, species_h, cells, head_flags, h_energy, h_force)
     barrier()
     e2e_t = []
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        eng.compute_flat(natoms, posn, species, cells, head_flags, h_energy, h_force)
+        eng.compute_flat(natoms, posn_h, species_h, cells, head_flags, h_energy, h_force)
         e2e_t.append(time.perf_counter() - t0)
     barrier()
     e2e_step = statistics.mean(e2e_t)
@@ -536,12 +552,24 @@ def main():
         sms = torch.cuda.get_device_properties(dev).multi_processor_count
         fp32_peak = sms * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
         ach = work["desc_flops"] / t_desc / 1e12
+        executed = None
+        ffile = os.path.join(REPO, "profiles", "flops.json")
+        if os.path.exists(ffile):
+            with open(ffile) as f:
+                fpa = json.load(f).get(WORKLOAD, {}).get("executed_fp32_flops_per_atom")
+            if fpa:
+                ex = fpa * total_atoms / t_desc / 1e12
+                executed = {"achieved": ex, "frac": ex / fp32_peak, "unit": "TFLOP/s",
+                            "work": "%d FP32 flops per atom executed (2 FFMA + FADD + FMUL, ncu instruction counts, "
+                                    "profiles/flops.json)" % fpa}
         roof = {"bound": "fp32", "kernel": "symm_kernel + force_kernel (descriptor and chain-rule triplet passes)",
                 "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak, "traffic": None,
                 "peak_source": "derived: %d SMs (from the device) x 128 FP32 lanes x 2 x sm_max_mhz from MEASURED_PEAKS.json "
                                "(no FP32 figure is measured)" % sms,
                 "work": "convention flops P*(30+13 nR) + T*(60+25 nA) = %.4g per step" % work["desc_flops"],
-                "kernel_ms": t_desc * 1000.0}
+                "kernel_ms": t_desc * 1000.0, "executed": executed,
+                "note": "achieved/frac count the fixed convention's flops, which the moment-tensor blocks no longer execute; "
+                        "executed.frac is the FP32 work the kernels actually issue"}
         tfile = os.path.join(REPO, "profiles", "traffic.json")
         if os.path.exists(tfile):
             with open(tfile) as f:
@@ -579,7 +607,8 @@ def main():
             "autotune": tune_report,
             "clocks": clk,
             "e2e": {"value": job / e2e_step, "unit": "atoms/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                    "ms_per_step": e2e_step * 1000},
+                    "ms_per_step": e2e_step * 1000,
+                    "path": "nnpgpu_compute on page-locked host arrays (positions, species, cells in; energies, forces out)"},
             "gpu_launches": KERNELS_PER_BATCH * args.steps,
             "roofline": roof,
             "kernels": kernels,
