@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
     const int ci = atom_cell[i] - S.cell0;
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
     // ranges 2q, 2q+1 of row q: start[] is monotone, so a run of cells is one slice of cell_atoms
-    int len[4];
+    int len[4], beg[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
       const int r = 4 * lane + t;
@@ -320,35 +320,83 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
         }
       }
       len[t] = n;
-      if (r < NB_RANGES) rb[r] = begin;
+      beg[t] = begin;
     }
+    // candidate numbering (prefix of the run lengths) and the non-empty runs compacted in order:
+    // rb[k], rp[k] = begin in cell_atoms and first candidate number of the k-th non-empty run
     const int lsum = len[0] + len[1] + len[2] + len[3];
-    int incl = lsum;
+    const int lne = (len[0] > 0) + (len[1] > 0) + (len[2] > 0) + (len[3] > 0);
+    int incl = lsum, incn = lne;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
+      const int w = __shfl_up_sync(0xffffffffu, incn, o);
+      if (lane >= o) {
+        incl += v;
+        incn += w;
+      }
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    int run = incl - lsum;
+    const int nne = __shfl_sync(0xffffffffu, incn, 31);
+    int run = incl - lsum, kk = incn - lne;
 #pragma unroll
     for (int t = 0; t < 4; ++t) {
-      rp[4 * lane + t] = run;
+      if (len[t] > 0) {
+        rb[kk] = beg[t];
+        rp[kk] = run;
+        ++kk;
+      }
       run += len[t];
     }
-    const int nr = 2 * nrow;
     __syncwarp();
+    // up to 32 * NB_MASK_WORDS candidates: a bit mask of the runs' first candidates and its word
+    // prefix (the ranking buffers, free until the lists are written) give a candidate's run as a
+    // rank, two independent shared-memory levels instead of a binary search
+    const bool by_rank = total <= 32 * NB_MASK_WORDS;
+    if (by_rank) {
+#pragma unroll
+      for (int t = 0; t < NB_MASK_WORDS / 32; ++t) msk[lane + 32 * t] = 0u;
+      __syncwarp();
+      for (int q = lane; q < nne; q += 32) atomicOr(&msk[rp[q] >> 5], 1u << (rp[q] & 31));
+      __syncwarp();
+      int wc[NB_MASK_WORDS / 32], ws = 0;
+#pragma unroll
+      for (int t = 0; t < NB_MASK_WORDS / 32; ++t) {
+        wc[t] = __popc(msk[4 * lane + t]);
+        ws += wc[t];
+      }
+      int winc = ws;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, winc, o);
+        if (lane >= o) winc += v;
+      }
+      int wrun = winc - ws;
+#pragma unroll
+      for (int t = 0; t < NB_MASK_WORDS / 32; ++t) {
+        wpre[4 * lane + t] = wrun;
+        wrun += wc[t];
+      }
+      __syncwarp();
+    }
     const float4 si = sfrac[i];
     const int4 fi = sfloor[i];
-    // candidate qd -> its position in cell_atoms: last range with prefix <= qd, then its slice
+    // candidate qd -> its position in cell_atoms: the last non-empty run starting at or before qd
     auto candidate = [&](int qd) -> int {
-      int lo = 0, hi = nr - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (rp[mid] <= qd) lo = mid;
-        else hi = mid - 1;
+      int kr;
+      if (by_rank) {
+        const int w = qd >> 5;
+        kr = wpre[w] + __popc(msk[w] & (0xffffffffu >> (31 - (qd & 31)))) - 1;
+      } else {
+        int lo = 0, hi = nne - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (rp[mid] <= qd) lo = mid;
+          else hi = mid - 1;
+        }
+        kr = lo;
       }
-      return rb[lo] + qd - rp[lo];
+      return rb[kr] + qd - rp[kr];
     };
     // the next chunk's candidates and coordinates are fetched while this chunk is decided; the
     // coordinates come from the cell-ordered copy (contiguous along a run)

@@ -183,7 +183,7 @@ __device__ __forceinline__ float act_d(int act, float a) {
   return (act == ACT_TANH) ? 1.0f - a * a : (act == ACT_SIGMOID) ? a * (1.0f - a) : 1.0f;
 }
 
-__global__ void __launch_bounds__(128, 1) network_tc_kernel(const __grid_constant__ TcNetsP N, int ntypes, const int* __restrict__ tc,
+__global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constant__ TcNetsP N, int ntypes, const int* __restrict__ tc,
                                                             const int* __restrict__ perm, const float* __restrict__ G, int gstride,
                                                             float* __restrict__ eatom, float* __restrict__ dEdG, int want_grad,
                                                             uint32_t tmem_cols, int opk, int pcols, int wait_limit,
