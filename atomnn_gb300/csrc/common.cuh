@@ -262,6 +262,21 @@ __device__ __forceinline__ float warp_sum(float v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+// Reduce-scatter of four per-lane values over the warp in five shuffles: afterwards the lanes
+// with (lane >> 3) & 3 == k hold the warp sum of v_k.
+__device__ __forceinline__ float warp_sum4(float v0, float v1, float v2, float v3) {
+  const int lane = threadIdx.x & 31;
+  const bool h16 = lane & 16, h8 = lane & 8;
+  float a = h16 ? v2 : v0, b = h16 ? v3 : v1;  // kept: the pair of values of this half
+  a += __shfl_xor_sync(0xffffffffu, h16 ? v0 : v2, 16);
+  b += __shfl_xor_sync(0xffffffffu, h16 ? v1 : v3, 16);
+  float k = h8 ? b : a;  // kept: one value of the pair
+  k += __shfl_xor_sync(0xffffffffu, h8 ? a : b, 8);
+  k += __shfl_xor_sync(0xffffffffu, k, 4);
+  k += __shfl_xor_sync(0xffffffffu, k, 2);
+  k += __shfl_xor_sync(0xffffffffu, k, 1);
+  return k;
+}
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -1248,10 +1248,10 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
           for (int k = 0; k < 4; ++k) acc[k] = fmaf(radial_value(R.phi, eta[k], rs[k], d), fc, acc[k]);
         }
       }
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const float v = warp_sum(acc[k]);
-        if (lane == 0 && f0 + k < R.n) Gi[R.off + f0 + k] = v * R.norm;
+      {
+        const float v = warp_sum4(acc[0], acc[1], acc[2], acc[3]);
+        const int k = (lane >> 3) & 3;
+        if ((lane & 7) == 0 && f0 + k < R.n) Gi[R.off + f0 + k] = v * R.norm;
       }
     }
   }
