@@ -49,11 +49,17 @@ struct RadialP {
 // has width e, 0 otherwise.  fn = 1 marks a block that leaves the grid (a zeta that is not a
 // power of two up to 2^(NZ_MAX-1), more than NE_MAX widths or NL lambdas): it takes the
 // per-function triplet path, and tab holds per function (1/eta^alpha, lambda, zeta, 0).
+// top = 1 marks a split GAUSS block: its functions with zeta <= MOM_N take
+// the moment path (mom = 1, their rows of M as above), the others all have the block's largest
+// zeta 2^(nz-1) and take the triplet path, which evaluates only that grid level (their rows of
+// M are zero).  When the centre type's moment blocks share their moments, the columns of M
+// follow the widths of block PotParams::mrep.
 struct AngP {
   int n, off, cut, alpha;
   float rc, pirc, rci, norm;
   int ne, nl, nz, mom;
   int moff, phi, tab, fn;
+  int top;
   float ietap[NE_MAX];
   float lam[NL];
   signed char gidx[NA_MAX];
@@ -72,8 +78,9 @@ struct PotParams {
   int ccut[NT_MAX];
   float crc[NT_MAX], cpirc[NT_MAX], crci[NT_MAX];
   // shared moments of centre type I (msh 1): its moment blocks (at most three) share one pair
-  // weight and involve the mns <= 2 neighbour species msp[I][0..mns); mrep is one of the blocks
-  // (its widths and pair weight stand for all); the stored moments are [set][width][MOM_C]
+  // weight and involve the mns <= 2 neighbour species msp[I][0..mns); mrep is the block with the
+  // most widths (the others' widths are among its, and its pair weight stands for all); the
+  // stored moments are [set][width of mrep][MOM_C]
   int msh[NT_MAX], mns[NT_MAX], mrep[NT_MAX];
   int msp[NT_MAX][2];
   RadialP rad[NT_MAX][NT_MAX];

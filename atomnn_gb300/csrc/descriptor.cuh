@@ -1,4 +1,4 @@
-// descriptor.cu - G2/G4 symmetry functions (NNP::symm, src/nnp/nnp.cpp:334-381) and their
+// descriptor.cuh - G2/G4 symmetry functions (NNP::symm, src/nnp/nnp.cpp:334-381) and their
 // chain rule into per-neighbour force contributions (NNP::force, src/nnp/nnp.cpp:416-482).
 //
 // One warp per centre atom.  The atom's neighbour slots are staged in shared memory, grouped
@@ -17,6 +17,10 @@
 // chain of squarings, and the force pass needs only three scalars per triplet (d/dcos, d/dr_ij,
 // d/dr_ik of sum_f dE/dG_f G_f).  The sum families IPOWS and SECHS evaluate their factor per
 // triplet.
+//
+// Device code only; the kernel instances and their launchers live in descriptor_symm.cu,
+// descriptor_force.cu, descriptor_force_gen.cu and descriptor_tangent.cu, which compile in parallel.
+#pragma once
 #include "common.cuh"
 #include "kernels.h"
 
@@ -102,9 +106,9 @@ __host__ __device__ constexpr float mom_mult(int a, int b, int c) {
 __host__ __device__ constexpr int mom_deg(int r) { return r < 1 ? 0 : (r < 4 ? 1 : (r < 10 ? 2 : (r < 20 ? 3 : 4))); }
 // mom_mult per component, and for each component q of degree <= 3 the components q + e_x,
 // q + e_y, q + e_z (runtime-indexed copies of the constexpr functions above)
-__device__ const float c_mom_mult[MOM_C] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 1, 1, 3, 3, 3, 6, 3, 1, 3,
+static __device__ const float c_mom_mult[MOM_C] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 1, 1, 3, 3, 3, 6, 3, 1, 3,
                                             3, 1, 1, 4, 4, 6, 12, 6, 4, 12, 12, 4, 1, 4, 6, 4, 1};
-__device__ const signed char c_mom_up[MOM_Q][3] = {{1, 2, 3},    {4, 5, 6},    {5, 7, 8},    {6, 8, 9},    {10, 11, 12},
+static __device__ const signed char c_mom_up[MOM_Q][3] = {{1, 2, 3},    {4, 5, 6},    {5, 7, 8},    {6, 8, 9},    {10, 11, 12},
                                                    {11, 13, 14}, {12, 14, 15}, {13, 16, 17}, {14, 17, 18}, {15, 18, 19},
                                                    {20, 21, 22}, {21, 23, 24}, {22, 24, 25}, {23, 26, 27}, {24, 27, 28},
                                                    {25, 28, 29}, {26, 30, 31}, {27, 31, 32}, {28, 32, 33}, {29, 33, 34}};
@@ -511,7 +515,7 @@ __device__ void force_mom_shared(const WarpSmem& S, const PotParams& P, int I, b
 
 // Stage the neighbour slots of atom i in shared memory, grouped by neighbour type.
 // Returns the number of staged slots; toff[t]..toff[t+1] is the range of type t.
-__device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, const int* __restrict__ type,
+static __device__ int stage_neighbors(const WarpSmem& S, int i, int cap, int ntypes, const int* __restrict__ type,
                                const int* __restrict__ nb_j, const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                const int* __restrict__ nb_cnt) {
   const int lane = threadIdx.x & 31;
@@ -626,16 +630,18 @@ __device__ __forceinline__ Sched make_sched(int J, int K, int j0, int nJ, int k0
 
 // G4 sums of one block on the (eta) x (lambda) x (zeta = 2^m) grid, NE x NL x NZ, written to
 // scratch[(e*NL+l)*NZ_MAX+m] (BasisA::symm, basis_angular.cpp:406-421; NNP::symm, nnp.cpp:359-377).
-template <int NE, int NZ>
+// TOP: only the level m = NZ-1 (the triplet part of a split block, AngP::top).
+template <int NE, int NZ, bool TOP>
 __device__ __forceinline__ void symm_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  constexpr int NC = TOP ? 1 : NZ, M0 = TOP ? NZ - 1 : 0;  // accumulated levels M0 .. M0+NC-1
   const int lane = threadIdx.x & 31;
-  float acc[NE][NL][NZ];
+  float acc[NE][NL][NC];
 #pragma unroll
   for (int e = 0; e < NE; ++e)
 #pragma unroll
     for (int l = 0; l < NL; ++l)
 #pragma unroll
-      for (int m = 0; m < NZ; ++m) acc[e][l][m] = 0.f;
+      for (int m = 0; m < NC; ++m) acc[e][l][m] = 0.f;
   const float lam0 = A.lam[0], lam1 = A.lam[1];
   const float* __restrict__ ux = S.ux;
   const float* __restrict__ uy = S.uy;
@@ -679,7 +685,7 @@ __device__ __forceinline__ void symm_block(const WarpSmem& S, const AngP& A, con
 #pragma unroll
         for (int l = 0; l < NL; ++l)
 #pragma unroll
-          for (int m = 0; m < NZ; ++m) acc[e][l][m] = fmaf(p2[l][m], E2, fmaf(p1[l][m], E1, acc[e][l][m]));
+          for (int m = 0; m < NC; ++m) acc[e][l][m] = fmaf(p2[l][M0 + m], E2, fmaf(p1[l][M0 + m], E1, acc[e][l][m]));
       }
     }
   }
@@ -688,9 +694,9 @@ __device__ __forceinline__ void symm_block(const WarpSmem& S, const AngP& A, con
 #pragma unroll
     for (int l = 0; l < NL; ++l)
 #pragma unroll
-      for (int m = 0; m < NZ; ++m) {
+      for (int m = 0; m < NC; ++m) {
         const float v = warp_sum(acc[e][l][m]);
-        if (lane == 0) S.scratch[(e * NL + l) * NZ_MAX + m] = v;
+        if (lane == 0) S.scratch[(e * NL + l) * NZ_MAX + M0 + m] = v;
       }
 }
 
@@ -700,22 +706,38 @@ __device__ __forceinline__ void symm_block(const WarpSmem& S, const AngP& A, con
 // registers; the partner's goes to shared memory (distinct partners within a round).
 // One triplet of the chain rule for owner a (registers) and partner b: returns the owner-side
 // vector in (oa*) and the partner-side vector in (ob*).
-template <int NE, int NZ>
+// TOP: only the level m = NZ-1, p^(2^(NZ-1)) and its derivative 2^(NZ-1) p^(2^(NZ-1)-1) from
+// the squaring chain and the running product of its terms.
+template <int NE, int NZ, bool TOP>
 __device__ __forceinline__ void chain_triplet(float uax, float uay, float uaz, float fa, float ga, float pa, float ia, const float* exa,
                                               float ubx, float uby, float ubz, float fb, float gb, float pb, float ib, const float* exb,
-                                              const float (&sg)[NE][NL][NZ], const float* ie, float lam0, float lam1, float hn, float nn,
-                                              float& oa0, float& oa1, float& oa2, float& ob0, float& ob1, float& ob2) {
+                                              const float (&sg)[NE][NL][TOP ? 1 : NZ], const float* ie, float lam0, float lam1, float hn,
+                                              float nn, float& oa0, float& oa1, float& oa2, float& ob0, float& ob1, float& ob2) {
+  constexpr int NC = TOP ? 1 : NZ;
   const float cs = uax * ubx + uay * uby + uaz * ubz;
-  float p[NL][NZ], qd[NL][NZ];
-  p[0][0] = fabsf(0.5f * (1.0f + lam0 * cs));
-  p[1][0] = fabsf(0.5f * (1.0f + lam1 * cs));
-#pragma unroll
-  for (int l = 0; l < NL; ++l) {
-    qd[l][0] = 1.0f;
+  float p[NL][NC], qd[NL][NC];
+  const float b0 = fabsf(0.5f * (1.0f + lam0 * cs)), b1 = fabsf(0.5f * (1.0f + lam1 * cs));
+  if constexpr (TOP) {
+    float x0 = b0, x1 = b1, r0 = 1.0f, r1 = 1.0f;
 #pragma unroll
     for (int m = 1; m < NZ; ++m) {
-      qd[l][m] = 2.0f * qd[l][m - 1] * p[l][m - 1];
-      p[l][m] = p[l][m - 1] * p[l][m - 1];
+      r0 *= x0; r1 *= x1;
+      x0 *= x0; x1 *= x1;
+    }
+    p[0][0] = x0; p[1][0] = x1;
+    qd[0][0] = (float)(1 << (NZ - 1)) * r0;
+    qd[1][0] = (float)(1 << (NZ - 1)) * r1;
+  } else {
+    p[0][0] = b0;
+    p[1][0] = b1;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      qd[l][0] = 1.0f;
+#pragma unroll
+      for (int m = 1; m < NZ; ++m) {
+        qd[l][m] = 2.0f * qd[l][m - 1] * p[l][m - 1];
+        p[l][m] = p[l][m - 1] * p[l][m - 1];
+      }
     }
   }
   float Q = 0.f, Q2 = 0.f, Pp = 0.f;
@@ -724,7 +746,7 @@ __device__ __forceinline__ void chain_triplet(float uax, float uay, float uaz, f
     const float E = exa[e] * exb[e];
     float q0 = 0.f, q1 = 0.f, r0 = 0.f, r1 = 0.f;
 #pragma unroll
-    for (int m = 0; m < NZ; ++m) {
+    for (int m = 0; m < NC; ++m) {
       q0 = fmaf(sg[e][0][m], p[0][m], q0);
       q1 = fmaf(sg[e][1][m], p[1][m], q1);
       r0 = fmaf(sg[e][0][m], qd[0][m], r0);
@@ -753,16 +775,17 @@ __device__ __forceinline__ void chain_triplet(float uax, float uay, float uaz, f
 // summed over the block's functions (BasisA::force, basis_angular.cpp:456-507), turned into the
 // neighbour-slot vectors of NNP::force (nnp.cpp:466-478).  The owner's vector accumulates in
 // registers; the partner's goes to shared memory (distinct partners within a round).
-template <int NE, int NZ>
+template <int NE, int NZ, bool TOP>
 __device__ __forceinline__ void force_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
+  constexpr int NC = TOP ? 1 : NZ, M0 = TOP ? NZ - 1 : 0;
   const int lane = threadIdx.x & 31;
-  float sg[NE][NL][NZ];
+  float sg[NE][NL][NC];
 #pragma unroll
   for (int e = 0; e < NE; ++e)
 #pragma unroll
     for (int l = 0; l < NL; ++l)
 #pragma unroll
-      for (int m = 0; m < NZ; ++m) sg[e][l][m] = S.scratch[(e * NL + l) * NZ_MAX + m];
+      for (int m = 0; m < NC; ++m) sg[e][l][m] = S.scratch[(e * NL + l) * NZ_MAX + M0 + m];
   float ie[NE];
 #pragma unroll
   for (int e = 0; e < NE; ++e) ie[e] = A.ietap[e];
@@ -798,8 +821,8 @@ __device__ __forceinline__ void force_block(const WarpSmem& S, const AngP& A, co
 #pragma unroll
         for (int e = 0; e < NE; ++e) exb[e] = ex[e * cap + b];
         float a0, a1, a2, c0, c1, c2;
-        chain_triplet<NE, NZ>(uax, uay, uaz, fa, ga, pa, ia, exa, ux[b], uy[b], uz[b], fc[b], gc[b], dpa[b], inv[b], exb, sg, ie, lam0,
-                              lam1, hn, nn, a0, a1, a2, c0, c1, c2);
+        chain_triplet<NE, NZ, TOP>(uax, uay, uaz, fa, ga, pa, ia, exa, ux[b], uy[b], uz[b], fc[b], gc[b], dpa[b], inv[b], exb, sg, ie,
+                                   lam0, lam1, hn, nn, a0, a1, a2, c0, c1, c2);
         w0 += a0; w1 += a1; w2 += a2;
         wx[b] += c0; wy[b] += c1; wz[b] += c2;
       }
@@ -989,7 +1012,7 @@ __device__ __forceinline__ float fn_radial(int phi, float ie, float da, float db
 }
 
 // G4 of a per-function block: FN_CHUNK functions per walk, written to Gi (times the norm).
-__device__ void symm_block_fn(const WarpSmem& S, const AngP& A, const float* __restrict__ ftab, const Sched& sc, float* Gi) {
+static __device__ void symm_block_fn(const WarpSmem& S, const AngP& A, const float* __restrict__ ftab, const Sched& sc, float* Gi) {
   const int lane = threadIdx.x & 31;
   for (int f0 = 0; f0 < A.n; f0 += FN_CHUNK) {
     float ie[FN_CHUNK], lam[FN_CHUNK], zeta[FN_CHUNK], acc[FN_CHUNK];
@@ -1034,7 +1057,7 @@ __device__ void symm_block_fn(const WarpSmem& S, const AngP& A, const float* __r
 // BasisA::force (basis_angular.cpp:456-640) with cw = |(1 + lambda cos)/2| and s = dE/dG_f:
 //   Q = sum s R cw^zeta,  Q2a/b = sum s ie k_a/b R cw^zeta,  Pp = sum s R lambda zeta cw^(zeta-1),
 // then phi, eta0, eta1 and the slot vectors as in force_block_gen.
-__device__ void force_block_fn(const WarpSmem& S, const AngP& A, const float* __restrict__ ftab, const Sched& sc, const float* gi) {
+static __device__ void force_block_fn(const WarpSmem& S, const AngP& A, const float* __restrict__ ftab, const Sched& sc, const float* gi) {
   const int lane = threadIdx.x & 31;
   const float hn = -0.5f * A.norm, nn = -A.norm;
   const float* __restrict__ sf = gi + A.off;
@@ -1110,13 +1133,31 @@ __device__ void run_block(const WarpSmem& S, const AngP& A, const Sched& sc, int
       return;
     }
   }
+  if (A.top) {  // the top level of a split block: exact nz
+#define NNP_TOP(NE_, NZ_)                                         \
+  case NE_ * 8 + NZ_:                                             \
+    if constexpr (NE_ <= NEK && NZ_ <= NZK) {                     \
+      if (FORCE) force_block<NE_, NZ_, true>(S, A, sc, cap);      \
+      else symm_block<NE_, NZ_, true>(S, A, sc, cap);             \
+    }                                                             \
+    break;
+    switch (A.ne * 8 + A.nz) {
+      NNP_TOP(1, 4) NNP_TOP(1, 5) NNP_TOP(1, 6)
+      NNP_TOP(2, 4) NNP_TOP(2, 5) NNP_TOP(2, 6)
+      NNP_TOP(3, 4) NNP_TOP(3, 5) NNP_TOP(3, 6)
+      NNP_TOP(4, 4) NNP_TOP(4, 5) NNP_TOP(4, 6)
+      default: break;
+    }
+#undef NNP_TOP
+    return;
+  }
   const int z = A.nz <= 3 ? 3 : (A.nz <= 5 ? 5 : 6);
   const int key = A.ne * 8 + z;
 #define NNP_CASE(NE_, NZ_)                                   \
   case NE_ * 8 + NZ_:                                        \
     if constexpr (NE_ <= NEK && NZ_ <= NZK) {                \
-      if (FORCE) force_block<NE_, NZ_>(S, A, sc, cap);       \
-      else symm_block<NE_, NZ_>(S, A, sc, cap);              \
+      if (FORCE) force_block<NE_, NZ_, false>(S, A, sc, cap); \
+      else symm_block<NE_, NZ_, false>(S, A, sc, cap);        \
     }                                                        \
     break;
   switch (key) {
@@ -1266,9 +1307,10 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (A.mom) {
-        if (msh) continue;
-        symm_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
-        continue;
+        if (!msh)
+          symm_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, mom ? mom + (size_t)i * mstride + A.moff : nullptr, Gi);
+        if (!A.top) continue;
+        __syncwarp();
       }
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, true);
       if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, true);
@@ -1282,7 +1324,10 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
       }
       run_block<false, NEK, NZK, GEN>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
-      for (int f = lane; f < A.n; f += 32) Gi[A.off + f] = A.norm * S.scratch[(int)P.atab[A.tab + f]];
+      for (int f = lane; f < A.n; f += 32) {
+        const int cell = (int)P.atab[A.tab + f];
+        if (!A.top || cell % NZ_MAX == A.nz - 1) Gi[A.off + f] = A.norm * S.scratch[cell];
+      }
       __syncwarp();
     }
 }
@@ -1370,9 +1415,9 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
       if (nJ == 0 || nK == 0 || (J == K && nJ < 2)) continue;
       if (A.mom) {
-        if (msh) continue;
-        force_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, gm + A.moff, gi);
-        continue;
+        if (!msh) force_mom_block<GEN>(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, gm + A.moff, gi);
+        if (!A.top) continue;
+        __syncwarp();
       }
       block_pair_factors<GEN>(S, A, j0, j0 + nJ, cap, false);
       if (K != J) block_pair_factors<GEN>(S, A, k0, k0 + nK, cap, false);
@@ -1561,61 +1606,9 @@ __global__ void __launch_bounds__(128) tangent_kernel(const __grid_constant__ Po
     }
 }
 
-template <int NEK, int NZK>
-static void launch_tangent_t(const BatchDev& B, const PotParams& P, const float4* tvec, float* U, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) attr = cudaFuncSetAttribute(tangent_kernel<NEK, NZK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  const int warps = 4;
-  tangent_kernel<NEK, NZK><<<(B.natoms + warps - 1) / warps, 32 * warps, sizeof(float) * warp_smem_floats(B.cap, NEK, true) * warps, st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_code, B.nb_cnt, tvec, U, B.gstride);
-}
 
-// The kernel instance must cover every block's zeta chain: the moment blocks' zeta <= 4 (nz 3)
-// included, which nz (the triplet blocks' largest) does not count.
-int launch_tangent(const BatchDev& B, const PotParams& P, int ne, int nz, const float4* tvec, float* U, cudaStream_t st) {
-  if (B.natoms == 0) return 0;
-  nz = nz < 3 ? 3 : nz;
-  if (ne <= 2 && nz <= 5) launch_tangent_t<2, 5>(B, P, tvec, U, st);
-  else if (ne <= 4 && nz <= 5) launch_tangent_t<4, 5>(B, P, tvec, U, st);
-  else if (ne <= 4 && nz <= 6) launch_tangent_t<4, 6>(B, P, tvec, U, st);
-  else return -1;
-  return 0;
-}
-
-size_t symm_smem_bytes(int cap, int ne, int warps) { return sizeof(float) * warp_smem_floats(cap, ne, false) * warps; }
-size_t force_smem_bytes(int cap, int ne, int warps, bool kx, int gstride) { return sizeof(float) * warp_smem_floats(cap, ne, kx, gstride) * warps; }
-
-template <int NEK, int NZK, bool GEN>
-static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  symm_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
-}
-template <int NEK, int NZK, bool GEN>
-static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  force_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, force_smem_bytes(B.cap, NEK, warps, GEN && P.kx, B.gstride + P.mstride), st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.W);
-}
-
-// Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).
-int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st) {
-  if (B.natoms == 0) return 0;
-  if (ne <= 2 && nz <= 5) P.gen ? launch_symm_t<2, 5, true>(B, P, warps, st) : launch_symm_t<2, 5, false>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 5) P.gen ? launch_symm_t<4, 5, true>(B, P, warps, st) : launch_symm_t<4, 5, false>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 6) P.gen ? launch_symm_t<4, 6, true>(B, P, warps, st) : launch_symm_t<4, 6, false>(B, P, warps, st);
-  else return -1;
-  return 0;
-}
-int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st) {
-  if (B.natoms == 0) return 0;
-  if (ne <= 2 && nz <= 5) P.gen ? launch_force_t<2, 5, true>(B, P, warps, st) : launch_force_t<2, 5, false>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 5) P.gen ? launch_force_t<4, 5, true>(B, P, warps, st) : launch_force_t<4, 5, false>(B, P, warps, st);
-  else if (ne <= 4 && nz <= 6) P.gen ? launch_force_t<4, 6, true>(B, P, warps, st) : launch_force_t<4, 6, false>(B, P, warps, st);
-  else return -1;
-  return 0;
-}
+// the force kernels of potentials with a non-GAUSS angular family (descriptor_force_gen.cu)
+int launch_force_gen(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
+size_t force_smem_bytes(int cap, int ne, int warps, bool kx, int gstride);
 
 }  // namespace nnpgpu

@@ -305,15 +305,27 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
       // factor is a product h(r_ij) h(r_ik)
       bool lam_ok = true;
       for (int l = 0; l < a.nl; ++l) lam_ok = lam_ok && std::fabs((double)lams[l]) <= 1.0;
-      if ((1 << (nz - 1)) <= MOM_N && lam_ok && !ang_sum_family(b.phi)) {
+      // a GAUSS block whose functions have zeta <= MOM_N or the block's largest zeta (above
+      // MOM_N) splits: the low ones take the moment path, the top level the triplet path
+      bool split = b.phi == ANG_GAUSS && lam_ok && (1 << (nz - 1)) > MOM_N;
+      bool any_low = false;
+      for (int f = 0; split && f < n; ++f) {
+        const int m = a.gidx[f] % NZ_MAX;
+        if ((1 << m) <= MOM_N) any_low = true;
+        else if (m != nz - 1) split = false;
+      }
+      split = split && any_low;
+      if (((1 << (nz - 1)) <= MOM_N && lam_ok && !ang_sum_family(b.phi)) || split) {
         int J = 0, K = 0;
         for (int x = 0; x < pot.ntypes; ++x)
           for (int y = x; y < pot.ntypes; ++y)
             if (lidx(x, y) == q) { J = x; K = y; }
         a.mom = 1;
+        a.top = split ? 1 : 0;
         a.moff = moff;
         moff += (J == K ? 1 : 2) * a.ne * MOM_C;
-      } else {
+      }
+      if (!a.mom || a.top) {
         nz_max = std::max(nz_max, nz);  // the triplet kernels' zeta chain covers triplet blocks only
         if (b.phi == ANG_IPOWP || b.phi == ANG_SECHP) P.kx = 1;
       }
@@ -328,11 +340,14 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
         if (P.ang[I][q].n > 0 && P.ang[I][q].mom) mq.push_back(q);
       bool ok = mq.size() >= 2;
       std::vector<int> sp;
+      int rep = ok ? mq[0] : 0;  // the block with the most widths
+      for (size_t t = 0; ok && t < mq.size(); ++t)
+        if (P.ang[I][mq[t]].ne > P.ang[I][rep].ne) rep = mq[t];
       for (size_t t = 0; ok && t < mq.size(); ++t) {
         const AngP& a = P.ang[I][mq[t]];
-        const AngP& r = P.ang[I][mq[0]];
-        ok = a.ne == r.ne && a.alpha == r.alpha && a.cut == r.cut && a.rc == r.rc && a.phi == r.phi;
-        for (int e = 0; ok && e < a.ne; ++e) ok = a.ietap[e] == r.ietap[e];
+        const AngP& r = P.ang[I][rep];
+        ok = a.alpha == r.alpha && a.cut == r.cut && a.rc == r.rc && a.phi == r.phi;
+        for (int e = 0; ok && e < a.ne; ++e) ok = std::find(r.ietap, r.ietap + r.ne, a.ietap[e]) != r.ietap + r.ne;
         for (int x = 0; x < pot.ntypes; ++x)
           for (int y = x; y < pot.ntypes; ++y)
             if (lidx(x, y) == mq[t]) {
@@ -345,9 +360,9 @@ void build_tables(const HPot& pot, PotParams& P, int& ne_max, int& nz_max) {
         std::sort(sp.begin(), sp.end());
         P.msh[I] = 1;
         P.mns[I] = (int)sp.size();
-        P.mrep[I] = mq[0];
+        P.mrep[I] = rep;
         for (int t = 0; t < 2; ++t) P.msp[I][t] = t < (int)sp.size() ? sp[t] : -1;
-        moff = P.mns[I] * P.ang[I][mq[0]].ne * MOM_C;  // the shared moments replace the per-block ones
+        moff = P.mns[I] * P.ang[I][rep].ne * MOM_C;  // the shared moments replace the per-block ones
       }
     }
     P.mstride = std::max(P.mstride, (moff + 3) / 4 * 4);
@@ -402,17 +417,22 @@ std::vector<float> build_ang_tables(const HPot& pot, PotParams& P) {
       }
       for (int f = 0; f < a.n; ++f) tab.push_back((float)a.gidx[f]);
       if (!a.mom) continue;
-      const int w = a.ne * (MOM_N + 1);
+      // columns follow the widths of the block whose moments this block reads: its own, or
+      // those of the centre type's representative block when the moments are shared
+      const AngP& L = P.msh[I] ? P.ang[I][P.mrep[I]] : a;
+      const int w = L.ne * (MOM_N + 1);
       const double norm = norm_value(b.norm, b.rc);
       for (int f = 0; f < a.n; ++f) {
         const int cell = a.gidx[f];
-        const int e = cell / (NL * NZ_MAX), m = cell % NZ_MAX, zeta = 1 << m;
+        const int m = cell % NZ_MAX, zeta = 1 << m;
+        const int e = (int)(std::find(L.ietap, L.ietap + L.ne, a.ietap[cell / (NL * NZ_MAX)]) - L.ietap);
         const double lam = a.lam[(cell / NZ_MAX) % NL];
-        // ((1 + lam c)/2)^zeta = sum_k binom(zeta, k) / 2^zeta lam^k c^k
+        // ((1 + lam c)/2)^zeta = sum_k binom(zeta, k) / 2^zeta lam^k c^k; functions of a split
+        // block's top level (zeta > MOM_N) are the triplet path's: zero rows
         for (int col = 0; col < w; ++col) {
           const int ce = col / (MOM_N + 1), k = col % (MOM_N + 1);
           double v = 0.0;
-          if (ce == e && k <= zeta) {
+          if (ce == e && k <= zeta && zeta <= MOM_N) {
             double binom = 1.0;
             for (int j = 0; j < k; ++j) binom = binom * (zeta - j) / (j + 1);
             v = norm * binom * std::pow(lam, k) / (double)(1 << zeta);

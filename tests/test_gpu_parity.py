@@ -298,19 +298,32 @@ def test_autotune_keeps_results(native_lib):
         eng.close()
 
 
-@pytest.mark.parametrize("variant", ["all_moment_blocks", "lambda_above_one"])
+@pytest.mark.parametrize("variant", ["all_moment_blocks", "lambda_above_one", "split_unshared", "split_top8", "split_top32",
+                                     "two_high_levels"])
 def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant):
     """Blocks with zeta <= 4 and |lambda| <= 1 run through the moment tensors, the others
     through the triplet loop.  all_moment_blocks: every block (the same-species A-A block
     included) on the moment path; lambda_above_one: lambda = 2 forces the triplet loop on
-    low-zeta blocks.  Both against the oracle on structures with one, few and many neighbours."""
+    low-zeta blocks.  GAUSS blocks whose other functions share the block's largest zeta split (low zeta on the moment path, the top level on the triplet loop):
+    split_unshared: two-width A-A blocks with zeta 1, 2, 4, 16 beside blocks of another width,
+    so that no moments are shared; split_top8 and split_top32: top levels zeta 8 and 32 (the
+    mixed512 potential itself splits its zeta-16 A-A blocks with shared moments);
+    two_high_levels: zeta 8 and 16 in one block, which keeps the whole block on the triplet loop.
+    All against the oracle on structures with one, few and many neighbours."""
     from atomnn_gb300 import engine
     pot = W.make_potential("mixed512")
     for (i, j, k), b in list(pot.angular.items()):
         if variant == "all_moment_blocks":
             pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [1, -1])
-        elif j != k:
-            pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [2, -1])
+        elif variant == "lambda_above_one":
+            if j != k:
+                pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [2, -1])
+        elif variant == "split_unshared":
+            pot.angular[(i, j, k)] = (W._angular(6.5, [0.005, 0.05], [1, 2, 4, 16], [1, -1]) if j == k == 0 else
+                                      W._angular(6.5, [0.02], [1, 2, 4], [1, -1]))
+        elif j == k == 0:
+            zetas = {"split_top8": [1, 2, 8], "split_top32": [1, 4, 32], "two_high_levels": [1, 8, 16]}[variant]
+            pot.angular[(i, j, k)] = W._angular(6.5, [0.005], zetas, [1, -1])
     for t in range(2):  # input sizes changed: new networks
         means = W._estimate_means(pot, t, 0.07, [1.0 / 3.0, 2.0 / 3.0])
         pot.nets[t] = W._make_network(np.random.default_rng(t), pot.ninput(t), [64, 64], means)
