@@ -406,31 +406,60 @@ __device__ void symm_mom_shared(const WarpSmem& S, const PotParams& P, int I, bo
   __syncwarp();
   if (gmom)
     for (int t = lane; t < ns * nec; t += 32) gmom[t] = MS[t];
+  // the moment blocks (at most three): species pairs packed 4 bits each, function counts 8 bits
+  int pk = 0, nk = 0, nb = 0, nf = 0;
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
-      if (A.n == 0 || !A.mom) continue;
-      const int sJ = mom_set(P, I, J), sK = mom_set(P, I, K);
-      float* V = S.scratch;
-      if (lane < ne * (MOM_N + 1)) {
-        const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
-        const float* MJ = MS + sJ * nec + e * MOM_C;
-        const float* MK = MS + sK * nec + e * MOM_C;
-        float v = 0.f;
-        for (int r = mom_off(n); r < mom_off(n + 1); ++r) v = fmaf(c_mom_mult[r] * MJ[r], MK[r], v);
-        if (J == K) v = 0.5f * (v - Dg[(sJ * ne + e) * (MOM_N + 1) + n]);
-        V[lane] = v;
-      }
-      __syncwarp();
-      const int w = ne * (MOM_N + 1);
-      const float* __restrict__ M = P.atab + A.tab + A.n;
-      for (int f = lane; f < A.n; f += 32) {
-        float v = 0.f;
-        for (int k = 0; k < w; ++k) v = fmaf(M[f * w + k], V[k], v);
-        Gi[A.off + f] = v;
-      }
-      __syncwarp();
+      if (A.n == 0 || !A.mom || nb >= 3) continue;
+      pk |= (J | (K << 2)) << (4 * nb);
+      nk |= A.n << (8 * nb);
+      nf += A.n;
+      ++nb;
     }
+  // inner products V[blk][e][n] of every block at once, lanes over (block, width, degree)
+  const int w = ne * (MOM_N + 1);
+  float* V = S.scratch;
+  for (int t = lane; t < nb * w; t += 32) {
+    const int k = t / w, c = t - k * w, e = c / (MOM_N + 1), n = c - e * (MOM_N + 1);
+    const int J = (pk >> (4 * k)) & 3, K = (pk >> (4 * k + 2)) & 3;
+    const int sJ = mom_set(P, I, J), sK = mom_set(P, I, K);
+    const float* MJ = MS + sJ * nec + e * MOM_C;
+    const float* MK = MS + sK * nec + e * MOM_C;
+    float v0 = 0.f, v1 = 0.f;
+    int r = mom_off(n);
+    const int r1 = mom_off(n + 1);
+    for (; r + 1 < r1; r += 2) {
+      v0 = fmaf(c_mom_mult[r] * MJ[r], MK[r], v0);
+      v1 = fmaf(c_mom_mult[r + 1] * MJ[r + 1], MK[r + 1], v1);
+    }
+    if (r < r1) v0 = fmaf(c_mom_mult[r] * MJ[r], MK[r], v0);
+    float v = v0 + v1;
+    if (J == K) v = 0.5f * (v - Dg[(sJ * ne + e) * (MOM_N + 1) + n]);
+    V[t] = v;
+  }
+  __syncwarp();
+  // every block's functions at once, lanes over (block, function): G_f = sum_c M[f][c] V[blk][c]
+  for (int t = lane; t < nf; t += 32) {
+    int k = 0, f = t;
+    while (k + 1 < nb && f >= ((nk >> (8 * k)) & 255)) {
+      f -= (nk >> (8 * k)) & 255;
+      ++k;
+    }
+    const AngP& A = P.ang[I][lidx((pk >> (4 * k)) & 3, (pk >> (4 * k + 2)) & 3)];
+    const float* __restrict__ M = P.atab + A.tab + A.n + f * w;
+    const float* Vk = V + k * w;
+    float g = 0.f;
+    for (int e = 0; e < ne; ++e) {  // one width (MOM_N + 1 columns) at a time, loads first
+      float m[MOM_N + 1];
+#pragma unroll
+      for (int c = 0; c <= MOM_N; ++c) m[c] = M[e * (MOM_N + 1) + c];
+#pragma unroll
+      for (int c = 0; c <= MOM_N; ++c) g = fmaf(m[c], Vk[e * (MOM_N + 1) + c], g);
+    }
+    Gi[A.off + f] = g;
+  }
+  __syncwarp();
 }
 
 // chain rule of every moment block of centre type I from the stored moments gm
@@ -447,44 +476,46 @@ __device__ void force_mom_shared(const WarpSmem& S, const PotParams& P, int I, b
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
       if (A.n == 0 || !A.mom || nb >= 3) continue;
-      float* b = S.scratch + 20 * nb;
-      const float* __restrict__ M = P.atab + A.tab + A.n;
-      if (lane < w) {
-        float s0 = 0.f, s1 = 0.f;
-        int f = 0;
-        for (; f + 1 < A.n; f += 2) {
-          s0 = fmaf(gi[A.off + f], M[f * w + lane], s0);
-          s1 = fmaf(gi[A.off + f + 1], M[(f + 1) * w + lane], s1);
-        }
-        if (f < A.n) s0 = fmaf(gi[A.off + f], M[f * w + lane], s0);
-        b[lane] = s0 + s1;
-      }
       pk |= (J | (K << 2)) << (4 * nb);
       ++nb;
     }
+  // every block at once, lanes over (block, column)
+  for (int t = lane; t < nb * w; t += 32) {
+    const int k = t / w, c = t - k * w;
+    const AngP& A = P.ang[I][lidx((pk >> (4 * k)) & 3, (pk >> (4 * k + 2)) & 3)];
+    const float* __restrict__ M = P.atab + A.tab + A.n + c;
+    const float* g = gi + A.off;
+    float s0 = 0.f, s1 = 0.f;
+    int f = 0;
+    for (; f + 1 < A.n; f += 2) {
+      s0 = fmaf(g[f], M[f * w], s0);
+      s1 = fmaf(g[f + 1], M[(f + 1) * w], s1);
+    }
+    if (f < A.n) s0 = fmaf(g[f], M[f * w], s0);
+    S.scratch[20 * k + c] = s0 + s1;
+  }
   __syncwarp();
   // tables of each species set: T_s[e][q] = sum over the blocks containing the species of
   // b_(deg q + 1) times the other species' moments one degree up; T0_s[e] likewise with degree 0
   float4* T = reinterpret_cast<float4*>(S.ex);
   float* T0 = S.scratch + 60;  // [set][e]
-  if (lane < MOM_Q) {
-    const int u0 = c_mom_up[lane][0], u1 = c_mom_up[lane][1], u2 = c_mom_up[lane][2], dq = mom_deg(lane) + 1;
-    for (int se = 0; se < ns * ne; ++se) {
-      const int set = se / ne, e = se % ne;
-      const int spc = P.msp[I][set];
-      float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
-      for (int k = 0; k < nb; ++k) {
-        const int bJ = (pk >> (4 * k)) & 3, bK = (pk >> (4 * k + 2)) & 3;
-        if (bJ != spc && bK != spc) continue;
-        const int other = bJ == spc ? bK : bJ;
-        const float bn = S.scratch[20 * k + e * (MOM_N + 1) + dq];
-        const float* Mg = gm + mom_set(P, I, other) * nec + e * MOM_C;
-        t.x = fmaf(bn, Mg[u0], t.x);
-        t.y = fmaf(bn, Mg[u1], t.y);
-        t.z = fmaf(bn, Mg[u2], t.z);
-      }
-      T[se * MOM_Q + lane] = t;
+  for (int v = lane; v < ns * ne * MOM_Q; v += 32) {
+    const int se = v / MOM_Q, q = v - se * MOM_Q;
+    const int u0 = c_mom_up[q][0], u1 = c_mom_up[q][1], u2 = c_mom_up[q][2], dq = mom_deg(q) + 1;
+    const int set = se / ne, e = se % ne;
+    const int spc = P.msp[I][set];
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int k = 0; k < nb; ++k) {
+      const int bJ = (pk >> (4 * k)) & 3, bK = (pk >> (4 * k + 2)) & 3;
+      if (bJ != spc && bK != spc) continue;
+      const int other = bJ == spc ? bK : bJ;
+      const float bn = S.scratch[20 * k + e * (MOM_N + 1) + dq];
+      const float* Mg = gm + mom_set(P, I, other) * nec + e * MOM_C;
+      t.x = fmaf(bn, Mg[u0], t.x);
+      t.y = fmaf(bn, Mg[u1], t.y);
+      t.z = fmaf(bn, Mg[u2], t.z);
     }
+    T[se * MOM_Q + q] = t;
   }
   if (lane < ns * ne) {
     const int set = lane / ne, e = lane % ne, spc = P.msp[I][set];

@@ -9,7 +9,8 @@ template <int NEK, int NZK, bool GEN>
 static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cudaStream_t st) {
   static bool attr = false;
   if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
-  symm_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, symm_smem_bytes(B.cap, NEK, warps), st>>>(
+  const size_t sm = symm_smem_bytes(B.cap, NEK, warps);
+  symm_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, sm, st>>>(
       P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
 }
 
