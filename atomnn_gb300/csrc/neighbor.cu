@@ -16,6 +16,21 @@
 
 namespace nnpgpu {
 
+// The fourth component of an atom's wrapped coordinates carries, as int bits, its species (bits
+// 0-1) and, when all three fit in 9 bits, its integer floors (bits 2-10, 11-19, 20-28, each +256;
+// bit 31 set): one 16-byte load then gives a candidate everything the single-image test needs.
+__device__ __forceinline__ int pack_w(int sp, int f0, int f1, int f2) {
+  const bool fit = f0 >= -256 && f0 < 256 && f1 >= -256 && f1 < 256 && f2 >= -256 && f2 < 256;
+  return fit ? (sp | ((f0 + 256) << 2) | ((f1 + 256) << 11) | ((f2 + 256) << 20) | (int)(1u << 31)) : sp;
+}
+__device__ __forceinline__ int w_species(const float4& s) { return __float_as_int(s.w) & 3; }
+// the floors of the atom whose wrapped coordinates are s: from s.w, else from its sfloor entry
+__device__ __forceinline__ int4 w_floors(const float4& s, const int4* __restrict__ sfl, int k) {
+  const unsigned w = (unsigned)__float_as_int(s.w);
+  if (!(w >> 31)) return sfl[k];
+  return make_int4((int)((w >> 2) & 511) - 256, (int)((w >> 11) & 511) - 256, (int)((w >> 20) & 511) - 256, 0);
+}
+
 // Wrapped fractional coordinates (FP32) and integer floors of R^-1 r, per atom.  Atoms of a
 // cell-list structure (mode 4) are also binned: atom_cell[i] and the cell's atom count.
 __global__ void frac_kernel(int a0, int natoms, int ntypes, const int* __restrict__ type, const double* __restrict__ posn,
@@ -48,7 +63,7 @@ __global__ void frac_kernel(int a0, int natoms, int ntypes, const int* __restric
   }  else {
     s = make_float4((float)p0, (float)p1, (float)p2, 0.f);
   }
-  s.w = __int_as_float(type ? clamp_type(type[i], ntypes) : 0);  // the species rides along for the lists
+  s.w = __int_as_float(pack_w(type ? clamp_type(type[i], ntypes) : 0, fl.x, fl.y, fl.z));
   sfrac[i] = s;
   sfloor[i] = fl;
   if (S.mode == 4) {
@@ -133,7 +148,7 @@ __device__ __forceinline__ void emit(int slot, int cap, int j, float rx, float r
     nb_j[slot] = j;
     nb_r[slot] = make_float4(rx, ry, rz, dr);
     nb_code[slot] = code;
-    if (nb_t) nb_t[slot] = (unsigned char)__float_as_int(sfrac[j].w);
+    if (nb_t) nb_t[slot] = (unsigned char)w_species(sfrac[j]);
   }
 }
 
@@ -192,7 +207,7 @@ __device__ __forceinline__ bool cell_diff_f32(const StrucMeta& S, const float4& 
 // j is kept when |diff|^2 <= rc^2.  FP32 from the wrapped fractional coordinates, with the FP64
 // replay of Cell::diff when |diff|^2 lies within the margin of rc^2.
 // sj = the candidate's wrapped coordinates, loaded by the caller ahead of use; its floors are
-// sfl[jf] (the atom's own entry, or its cell-ordered copy).
+// packed in sj.w, or else sfl[jf] (the atom's own entry, or its cell-ordered copy).
 __device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& si, const int4& fi, int j, const float4 sj,
                                              const int4* __restrict__ sfl, int jf, const double* __restrict__ posn, double pi0, double pi1,
                                              double pi2, double rc2, float rc2f, float m, float& r0, float& r1, float& r2, float& dr,
@@ -203,7 +218,7 @@ __device__ __forceinline__ bool single_image(const StrucMeta& S, const float4& s
   rf_mul(S, dl0 - q0, dl1 - q1, dl2 - q2, r0, r1, r2);
   const float d2f = r0 * r0 + r1 * r1 + r2 * r2;
   if (d2f > rc2f + m) return false;
-  const int4 fj = sfl[jf];
+  const int4 fj = w_floors(sj, sfl, jf);
   D[0] = k0 + fi.x - fj.x;
   D[1] = k1 + fi.y - fj.y;
   D[2] = k2 + fi.z - fj.z;
@@ -420,7 +435,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       const unsigned mk = __ballot_sync(0xffffffffu, keep);
       const int slot = count + __popc(mk & lt);
       if (keep && slot < cap) {
-        st_j[slot] = j | (__float_as_int(sj.w) << 30);  // species in the top two bits
+        st_j[slot] = j | (w_species(sj) << 30);  // species in the top two bits
         st_r[slot] = make_float4(r0, r1, r2, dr);
         st_c[slot] = pack_code(D[0], D[1], D[2], true);
       }
@@ -500,7 +515,7 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
         T[2] = code_t(code, 2);
         j = j0 + jl;
         const float4 sj = sfrac[j];
-        const int4 fj = sfloor[j];
+        const int4 fj = w_floors(sj, sfloor, j);
         // f_i - f_j - T = (s_i - s_j) + (floor_i - floor_j - T): the integer part is exact
         const float d0 = (si.x - sj.x) + (float)(fi.x - fj.x - T[0]);
         const float d1 = (si.y - sj.y) + (float)(fi.y - fj.y - T[1]);
@@ -542,7 +557,8 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
       // coordinates, visited in the reference's order (image n = ((a+s0)(2s1+1) + b+s1)(2s2+1) + c+s2)
       int lo[3] = {0, 0, 0}, hi[3] = {-1, -1, -1};
       if (jl < nj) {
-        bool ok = cell_diff_f32(S, si, fi, sfrac[j], sfloor[j], o0, o1, o2, D);
+        const float4 sj = sfrac[j];
+        bool ok = cell_diff_f32(S, si, fi, sj, w_floors(sj, sfloor, j), o0, o1, o2, D);
         if (ok) {
           const float fr[3] = {S.rinvf[0] * o0 + S.rinvf[3] * o1 + S.rinvf[6] * o2, S.rinvf[1] * o0 + S.rinvf[4] * o1 + S.rinvf[7] * o2,
                                S.rinvf[2] * o0 + S.rinvf[5] * o1 + S.rinvf[8] * o2};
