@@ -146,8 +146,12 @@ struct ImgEntry {
 };
 
 // Device status words (one int array per context).
-enum { ST_MAXCOUNT = 0, ST_ORPHANS = 1, ST_ERROR = 2, ST_DEBUG = 8, ST_WORDS = 32 };
-enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_ORPHANS = 4, ERR_TIMEOUT = 8, ERR_DRAIN = 16 };
+// Forces are summed in 64-bit fixed point with FORCE_FRAC_BITS fractional bits (2^-32 eV/A): each
+// neighbour slot's FP32 contribution is rounded once to that grid, and integer sums are exact and
+// commutative, so a force does not depend on the order in which warps add to it.
+constexpr int FORCE_FRAC_BITS = 32;
+enum { ST_MAXCOUNT = 0, ST_ERROR = 2, ST_DEBUG = 8, ST_WORDS = 32 };
+enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_TIMEOUT = 8, ERR_DRAIN = 16 };
 
 #ifdef __CUDACC__
 // ---- exact FP64 helpers: fixed evaluation order and no FMA contraction, so that the GPU
@@ -210,6 +214,16 @@ __host__ __device__ inline bool code_min(int c) { return (c >> 30) & 1; }
 __host__ __device__ inline int code_t(int c, int k) { return ((c >> (10 * k)) & 0x3ff) - 512; }
 
 #ifdef __CUDACC__
+// Asynchronous 16-byte global -> shared copies (cp.async), committed in groups and waited
+// for by group count: rows and candidates are requested ahead of the instruction that reads them.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // Round to nearest, ties to even (as rintf), for |x| < 2^22, with plain FP32 adds: adding
 // 1.5*2^23 leaves the rounded integer in the low mantissa bits.  k receives it as an int.
 __device__ __forceinline__ float round_even(float x, int& k) {
@@ -284,6 +298,14 @@ __device__ __forceinline__ float warp_sum4(float v0, float v1, float v2, float v
   k += __shfl_xor_sync(0xffffffffu, k, 1);
   return k;
 }
+__device__ __forceinline__ long long force_fixed(float w) { return __float2ll_rn(w * (float)(1ull << FORCE_FRAC_BITS)); }
+__device__ __forceinline__ long long warp_sum_ll(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+// fire-and-forget 64-bit integer add (two's complement: negative values subtract)
+__device__ __forceinline__ void red_add(long long* p, long long v) { atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)v); }
 __device__ __forceinline__ double warp_sum_d(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

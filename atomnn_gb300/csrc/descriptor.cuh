@@ -60,15 +60,6 @@ __device__ inline WarpSmem carve(float* base, int cap, int ne, bool kx) {
   return s;
 }
 
-// Asynchronous 16-byte global -> shared copies (cp.async): the row of a centre is requested at
-// the start of the kernel and waited for where it is first used.
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ float powi(float x, int a) {
   float y = 1.f;
@@ -1369,7 +1360,8 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
                                                     const int* __restrict__ type, const int* __restrict__ nb_j,
                                                     const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                                     const int* __restrict__ nb_cnt, const float* __restrict__ dEdG, int gstride,
-                                                    const float* __restrict__ mom, int mstride, float4* __restrict__ W) {
+                                                    const float* __restrict__ mom, int mstride, const int* __restrict__ nb_code,
+                                                    long long* __restrict__ facc) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
@@ -1472,9 +1464,27 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
       __syncwarp();
     }
 
-  // write the per-slot contributions in the list's own slot order
-  float4* Wi = W + (size_t)i * cap;
-  for (int p = lane; p < n; p += 32) Wi[S.orig[p]] = make_float4(S.wx[p], S.wy[p], S.wz[p], 0.f);
+  // NNP::force (nnp.cpp:466-478): the centre gains every slot's vector and the neighbour of a
+  // minimum-image slot loses it, summed in fixed point (each slot rounded once; the neighbours'
+  // adds arrive from other warps in any order, and integer sums do not depend on it)
+  long long ox = 0, oy = 0, oz = 0;
+  for (int p = lane; p < n; p += 32) {
+    const long long qx = force_fixed(S.wx[p]), qy = force_fixed(S.wy[p]), qz = force_fixed(S.wz[p]);
+    ox += qx;
+    oy += qy;
+    oz += qz;
+    const size_t g = (size_t)i * cap + S.orig[p];
+    if (code_min(nb_code[g])) {
+      long long* fj = facc + 3 * (size_t)nb_j[g];
+      red_add(fj, -qx);
+      red_add(fj + 1, -qy);
+      red_add(fj + 2, -qz);
+    }
+  }
+  ox = warp_sum_ll(ox);
+  oy = warp_sum_ll(oy);
+  oz = warp_sum_ll(oz);
+  if (lane < 3) red_add(facc + 3 * (size_t)i + lane, lane == 0 ? ox : (lane == 1 ? oy : oz));
 }
 
 // ------------------------------------------------------------------------------------ tangent

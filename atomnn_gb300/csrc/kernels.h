@@ -30,7 +30,6 @@ struct BatchDev {
   int* nb_code = nullptr;
   unsigned char* nb_t = nullptr;  // species of each slot's neighbour (null: looked up from type[])
   int* nb_cnt = nullptr;
-  int* nb_rev = nullptr;
   // cell lists of the structures in neighbour mode 4 (ncells entries, sentinels included)
   int ncells = 0;
   int* cell_cnt = nullptr;    // atoms per cell; zero between calls
@@ -39,8 +38,6 @@ struct BatchDev {
   int* atom_cell = nullptr;   // [natoms] cell of each atom
   float4* sfrac_c = nullptr;  // [natoms] sfrac in cell_atoms order
   int4* sfloor_c = nullptr;   // [natoms] sfloor in cell_atoms order
-  int* orphans = nullptr;
-  int orphan_cap = 0;
   // descriptors and networks
   float* G = nullptr;      // [natoms*gstride]
   float* dEdG = nullptr;   // [natoms*gstride]
@@ -50,7 +47,7 @@ struct BatchDev {
   int* perm = nullptr;     // [natoms] atoms grouped by type
   int* type_count = nullptr;  // [NT_MAX+1] counters (device)
   // forces
-  float4* W = nullptr;     // [natoms*cap] per-slot gradient contribution
+  long long* facc = nullptr;  // [natoms*3] forces in 64-bit fixed point (FORCE_SCALE units), summed by the chain rule
   double* force = nullptr; // [natoms*3] output
   double* energy = nullptr;  // [nstruc] output
   int* status = nullptr;   // [ST_WORDS]
@@ -69,7 +66,6 @@ struct TuneCfg {
 void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps = 4);
 // dynamic shared memory of the neighbour kernel when some structure uses a cell list
 size_t neighbor_smem_bytes(int cap, int warps);
-void launch_reverse(const BatchDev& B, cudaStream_t st);
 // descriptors (NNP::symm) and chain rule (NNP::force) ; ne/nz select the template instance
 int launch_symm(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
 int launch_force(const BatchDev& B, const PotParams& P, int ne, int nz, int warps, cudaStream_t st);
@@ -113,7 +109,7 @@ void launch_train_force_loss(const BatchDev& B, const double* fref, double beta,
 int launch_tangent(const BatchDev& B, const PotParams& P, int ne, int nz, const float4* tvec, float* U, cudaStream_t st);
 int launch_train_force(const BatchDev& B, const NetsP& N, int ntypes, const float* U, float* partial, int pstride, double* grad,
                        int max_params, cudaStream_t st);
-// force gather, orphan fix-up, per-structure energy
+// forces from their fixed-point sums, per-structure energy
 void launch_gather(const BatchDev& B, const NetsP& N, bool add_vacuum, bool want_force, cudaStream_t st);
 
 }  // namespace nnpgpu

@@ -686,102 +686,6 @@ __global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int c
   }
 }
 
-// Transposed index for the force gather.  For every minimum-image slot (i,s) -> j, find the
-// minimum-image slot of j's list that points back to i and store there the global slot id of
-// (i,s).  Lists are sorted by neighbour index, so each lane binary-searches its own target.
-// A source without a partner (possible only for pairs within rounding of the cutoff, or ties
-// between equidistant images) is recorded as an orphan and added by a serial fix-up pass.
-// The minimum-image slots of a pair point at each other (each list holds one minimum-image
-// entry per neighbour), so pass 0 searches only from the lower index (i < j) and on a match sets
-// both entries; pass 1 visits the slots with i > j and searches only where pass 0 left no entry.
-__global__ void __launch_bounds__(128) reverse_kernel(int a0, int natoms, int cap, const int* __restrict__ nb_j,
-                                                      const int* __restrict__ nb_code, const int* __restrict__ nb_cnt,
-                                                      int* __restrict__ nb_rev, int* __restrict__ orphans, int orphan_cap,
-                                                      int* __restrict__ status, int pass) {
-  const int lane = threadIdx.x & 31;
-  const int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (i >= a0 + natoms) return;
-  const int n = min(nb_cnt[i], cap);
-  if (pass == 1) {
-    // what pass 0 left: a slot already paired is skipped on its reverse entry alone
-    for (int s = lane; s < n; s += 32) {
-      const size_t src = (size_t)i * cap + s;
-      if (nb_rev[src] >= 0 || !code_min(nb_code[src])) continue;
-      const int j = nb_j[src];
-      if (i < j) continue;
-      const int nj = min(nb_cnt[j], cap);
-      const int* L = nb_j + (size_t)j * cap;
-      int lo = 0, hi = nj;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (L[mid] < i) lo = mid + 1;
-        else hi = mid;
-      }
-      int found = -1;
-      for (int t = lo; t < nj && L[t] == i; ++t)
-        if (code_min(nb_code[(size_t)j * cap + t])) { found = t; break; }
-      if (found >= 0) {
-        nb_rev[(size_t)j * cap + found] = (int)src;
-      } else {
-        const int k = atomicAdd(&status[ST_ORPHANS], 1);
-        if (k < orphan_cap) orphans[k] = (int)src;
-      }
-    }
-    return;
-  }
-  // pass 0: RS slots per lane at a time, their binary searches advanced in lockstep so that the
-  // dependent loads of different searches overlap
-  constexpr int RS = 4;
-  for (int s0 = lane; s0 < n; s0 += 32 * RS) {
-    int tj[RS], lo[RS], hi[RS];
-#pragma unroll
-    for (int k = 0; k < RS; ++k) {
-      const int s = s0 + 32 * k;
-      tj[k] = -1;
-      lo[k] = 0;
-      hi[k] = 0;
-      if (s < n) {
-        const size_t src = (size_t)i * cap + s;
-        const int j = nb_j[src];
-        if (code_min(nb_code[src]) && i < j) {
-          tj[k] = j;
-          hi[k] = min(nb_cnt[j], cap);
-        }
-      }
-    }
-    bool more = true;
-    while (more) {
-      more = false;
-#pragma unroll
-      for (int k = 0; k < RS; ++k)
-        if (lo[k] < hi[k]) {
-          const int mid = (lo[k] + hi[k]) >> 1;
-          if (nb_j[(size_t)tj[k] * cap + mid] < i) lo[k] = mid + 1;
-          else hi[k] = mid;
-          more = more || lo[k] < hi[k];
-        }
-    }
-#pragma unroll
-    for (int k = 0; k < RS; ++k) {
-      if (tj[k] < 0) continue;
-      const int j = tj[k];
-      const size_t src = (size_t)i * cap + s0 + 32 * k;
-      const int nj = min(nb_cnt[j], cap);
-      const int* L = nb_j + (size_t)j * cap;
-      int found = -1;
-      for (int t = lo[k]; t < nj && L[t] == i; ++t)
-        if (code_min(nb_code[(size_t)j * cap + t])) { found = t; break; }
-      if (found >= 0) {
-        nb_rev[(size_t)j * cap + found] = (int)src;
-        nb_rev[src] = (int)((size_t)j * cap + found);
-      } else {
-        const int o = atomicAdd(&status[ST_ORPHANS], 1);
-        if (o < orphan_cap) orphans[o] = (int)src;
-      }
-    }
-  }
-}
-
 void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   warps = warps < 1 ? 1 : (warps > 4 ? 4 : warps);
   if (B.natoms == 0) return;
@@ -800,14 +704,6 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
                                              B.atom_cell, B.cell_start, B.cell_atoms, B.sfrac_c, B.sfloor_c, B.nb_j, B.nb_r, B.nb_code, B.nb_t,
                                              B.nb_cnt, B.status);
-}
-
-void launch_reverse(const BatchDev& B, cudaStream_t st) {
-  if (B.natoms == 0) return;
-  cudaMemsetAsync(B.nb_rev + (size_t)B.a0 * B.cap, 0xff, sizeof(int) * (size_t)B.natoms * B.cap, st);
-  for (int pass = 0; pass < 2; ++pass)
-    reverse_kernel<<<(B.natoms + 3) / 4, 128, 0, st>>>(B.a0, B.natoms, B.cap, B.nb_j, B.nb_code, B.nb_cnt, B.nb_rev, B.orphans,
-                                                       B.orphan_cap, B.status, pass);
 }
 
 }  // namespace nnpgpu

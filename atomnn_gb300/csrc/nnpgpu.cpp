@@ -224,7 +224,7 @@ int run_pipeline(nnpgpu_ctx* c, const BatchDev& B, int flags, cudaStream_t st) {
   mark(0);
   launch_neighbors(B, st, c->tune.warps_nbr);
   mark(1);
-  if (want_force) launch_reverse(B, st);
+  if (want_force) cudaMemsetAsync(B.facc + 3 * (size_t)B.a0, 0, sizeof(long long) * 3 * (size_t)B.natoms, st);
   mark(2);
   if (launch_symm(B, c->P, c->ne, c->nz, c->tune.warps_symm, st) != 0) return set_error(c, NNPGPU_ERR_UNSUPPORTED, "no symm kernel instance");
   mark(3);
@@ -325,10 +325,10 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
        ensure(c, c->imgs, sizeof(ImgEntry) * imgs.size()) && ensure(c, c->sfrac, sizeof(float4) * N) && ensure(c, c->sfloor, sizeof(int4) * N) &&
        ensure(c, c->nb_j, sizeof(int) * NC) && ensure(c, c->nb_r, sizeof(float4) * NC) && ensure(c, c->nb_code, sizeof(int) * NC) &&
        ensure(c, c->nb_t, NC) &&
-       ensure(c, c->nb_cnt, sizeof(int) * N) && ensure(c, c->nb_rev, sizeof(int) * NC) && ensure(c, c->orphans, sizeof(int) * N) &&
+       ensure(c, c->nb_cnt, sizeof(int) * N) &&
        ensure(c, c->G, sizeof(float) * N * c->gstride) && ensure(c, c->dEdG, sizeof(float) * N * c->gstride) &&
        ensure(c, c->eatom, sizeof(float) * N) && ensure(c, c->perm, sizeof(int) * N) &&
-       ensure(c, c->type_count, sizeof(int) * type_sort_ints((int)N)) && ensure(c, c->W, sizeof(float4) * NC) &&
+       ensure(c, c->type_count, sizeof(int) * type_sort_ints((int)N)) && ensure(c, c->facc, sizeof(long long) * 3 * N) &&
        ensure(c, c->force, sizeof(double) * 3 * N) && ensure(c, c->energy, sizeof(double) * std::max(nstruc, 1)) &&
        ensure(c, c->status, sizeof(int) * ST_WORDS) && (c->P.mstride == 0 || ensure(c, c->mom, sizeof(float) * N * c->P.mstride));
   if (ok && U.ncells > 0) {
@@ -393,7 +393,6 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.nb_code = (int*)c->nb_code.p;
   B.nb_t = (unsigned char*)c->nb_t.p;
   B.nb_cnt = (int*)c->nb_cnt.p;
-  B.nb_rev = (int*)c->nb_rev.p;
   B.ncells = U.ncells;
   if (U.ncells > 0) {
     B.cell_cnt = (int*)c->cell_cnt.p;
@@ -403,8 +402,6 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
     B.sfrac_c = (float4*)c->sfrac_c.p;
     B.sfloor_c = (int4*)c->sfloor_c.p;
   }
-  B.orphans = (int*)c->orphans.p;
-  B.orphan_cap = std::max(U.natoms, 1);
   B.G = (float*)c->G.p;
   B.dEdG = (float*)c->dEdG.p;
   B.mom = (float*)c->mom.p;
@@ -412,7 +409,7 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.eatom = (float*)c->eatom.p;
   B.perm = (int*)c->perm.p;
   B.type_count = (int*)c->type_count.p;
-  B.W = (float4*)c->W.p;
+  B.facc = (long long*)c->facc.p;
   B.force = force;
   B.energy = energy;
   B.status = (int*)c->status.p;
@@ -492,7 +489,6 @@ int check_status(nnpgpu_ctx* c, const int* st_words, int cap) {
                      "a bounded wait on the device ran out and the kernel's own copies did not finish either (tensor-core network); "
                      "destroy this context");
   if (st_words[ST_ERROR] & ERR_TIMEOUT) return set_error(c, NNPGPU_ERR_TIMEOUT, "a bounded wait on the device ran out (tensor-core network)");
-  if (st_words[ST_ERROR] & ERR_ORPHANS) return set_error(c, NNPGPU_ERR_INVALID, "inconsistent neighbour lists (too many unmatched minimum images)");
   if (st_words[ST_MAXCOUNT] > cap) {
     const int need = (st_words[ST_MAXCOUNT] + 31) / 32 * 32;
     if (need > 256) return set_error(c, NNPGPU_ERR_CAPACITY, "more than 256 neighbours within the cutoff for some atom");
@@ -601,7 +597,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   c->serving.reset();
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
-                    &c->nb_rev, &c->orphans, &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->W, &c->force, &c->energy,
+                    &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->facc, &c->force, &c->energy,
                     &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
                     &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in, &c->tr_fref, &c->tr_t,
                     &c->tr_fatom, &c->tr_fstruc, &c->tr_u, &c->sfrac_c, &c->sfloor_c};
@@ -641,7 +637,7 @@ extern "C" int nnpgpu_profile_read(const nnpgpu_ctx* c, int stage, double* total
 }
 
 extern "C" const char* nnpgpu_profile_stage_name(int stage) {
-  static const char* names[NNPGPU_NSTAGES] = {"neighbors", "transpose", "descriptors", "networks", "chain_rule", "gather_energy"};
+  static const char* names[NNPGPU_NSTAGES] = {"neighbors", "force_clear", "descriptors", "networks", "chain_rule", "forces_energy"};
   return (stage >= 0 && stage < NNPGPU_NSTAGES) ? names[stage] : "?";
 }
 

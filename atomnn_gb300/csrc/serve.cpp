@@ -100,7 +100,9 @@ struct Serving::Impl {
   }
 
   // bytes of device state one atom needs inside a batch (neighbour slots dominate)
-  static size_t bytes_per_atom(int cap, int gstride) { return (size_t)cap * 48 + (size_t)gstride * 8 + 160; }
+  // (slot index, vector, image code, species: 25 B; per atom coordinates, floors, fixed-point and
+  // FP64 forces, counts and the network rows)
+  static size_t bytes_per_atom(int cap, int gstride) { return (size_t)cap * 28 + (size_t)gstride * 8 + 200; }
 
   bool can_use_skin(const Resident& r, const Req& q) const {
     if (!r.d_j || r.natoms != q.natoms || r.species != q.species) return false;

@@ -4,7 +4,7 @@
 A step is one evaluation of energy and forces of every structure of the workload ``mixed512``
 (512 seeded triclinic two-species structures, 16-2048 atoms, log-uniform; 24 G2 + 32 G4 per
 species; networks 56-64-64-1): neighbour lists, symmetry functions, atomic networks, chain
-rule and force gather, all on the GPU.  ``value`` is atoms/s with inputs resident in HBM;
+rule and force sums, all on the GPU.  ``value`` is atoms/s with inputs resident in HBM;
 ``e2e`` is the same through the host-buffer C API (copies inside the timed region).
 
 ``--impl reference`` times the reference algorithm on the host CPU cores instead: the FP64 C++
@@ -37,7 +37,7 @@ from atomnn_gb300 import workloads as W  # noqa: E402
 
 METRIC = "atoms/sec E+F (BF16 batched vs plain), p50/p99 latency, at force err ≤1e-3 eV/Å"
 WORKLOAD = "mixed512"
-KERNELS_PER_BATCH = 15  # frac, cell scan, cell fill, neighbor, 2x reverse, symm, 3x type sort, network, force, gather, orphan, energy
+KERNELS_PER_BATCH = 12  # frac, cell scan, cell fill, neighbor, symm, 3x type sort, network, force, force conversion, energy
 WORK_DIR = os.path.join(REPO, "atomnn_gb300", "_build", "workloads")
 
 
@@ -137,8 +137,8 @@ def dist_info():
 
 def convention_work(eng, strucs, pot):
     """Algorithmic work of one step in the fixed convention: FP32 flops of descriptors+chain rule
-    = P*(30 + 13*nR_J) + T*(60 + 25*nA_JK); neighbour bytes = 16N + 16P + 4N; gather bytes =
-    28P + 24N; network flops = 4*sum_l in_l*out_l per atom."""
+    = P*(30 + 13*nR_J) + T*(60 + 25*nA_JK); neighbour bytes = 16N + 16P + 4N; force and energy bytes =
+    52N (fixed-point sums in, FP64 forces out, atomic energies in); network flops = 4*sum_l in_l*out_l per atom."""
     nt = pot.ntypes
     nR = [[len(pot.radial[(i, j)].rs) for j in range(nt)] for i in range(nt)]
     nA = {(i, j, k): len(pot.angular[(i, j, k)].eta) for i in range(nt) for j in range(nt) for k in range(j, nt)}
@@ -163,7 +163,7 @@ def convention_work(eng, strucs, pot):
             net = pot.nets[I]
             dims = [net.nin] + list(net.nodes)
             net_flops += n * 4 * sum(dims[l] * dims[l + 1] for l in range(len(dims) - 1))
-    return dict(pairs=P, atoms=N, desc_flops=flops_desc, nbr_bytes=16 * N + 16 * P + 4 * N, gather_bytes=28 * P + 24 * N,
+    return dict(pairs=P, atoms=N, desc_flops=flops_desc, nbr_bytes=16 * N + 16 * P + 4 * N, gather_bytes=52 * N,
                 net_flops=net_flops)
 
 
@@ -578,11 +578,11 @@ def main():
         kernels = {
             "neighbors": {"bound": "hbm", "achieved_gbs": work["nbr_bytes"] / (stage["neighbors"] / 1000) / 1e9, "peak_gbs": hbm,
                           "ms": stage["neighbors"]},
-            "gather_energy": {"bound": "hbm", "achieved_gbs": work["gather_bytes"] / (stage["gather_energy"] / 1000) / 1e9,
-                              "peak_gbs": hbm, "ms": stage["gather_energy"]},
+            "forces_energy": {"bound": "hbm", "achieved_gbs": work["gather_bytes"] / (stage["forces_energy"] / 1000) / 1e9,
+                              "peak_gbs": hbm, "ms": stage["forces_energy"]},
             "networks": {"bound": "tensor" if bf16_ok else "fp32", "achieved_tflops": work["net_flops"] / (stage["networks"] / 1000) / 1e12,
                          "peak_tflops": pk["bf16_tflops"] if bf16_ok else fp32_peak, "ms": stage["networks"]},
-            "descriptors": {"ms": stage["descriptors"]}, "chain_rule": {"ms": stage["chain_rule"]}, "transpose": {"ms": stage["transpose"]},
+            "descriptors": {"ms": stage["descriptors"]}, "chain_rule": {"ms": stage["chain_rule"]}, "force_clear": {"ms": stage["force_clear"]},
         }
         acc = None
         if cpu is not None:

@@ -120,7 +120,7 @@ int nnpgpu_symm_noalloc(nnpgpu_ctx* ctx, int natoms, const double* d_posn, const
 /* ---- stage tracing (diagnostics; the reference times phases with util/Clock, e.g.
  * src/nnp/nnpte.cpp:1971-1990).  When enabled, CUDA events bracket each stage of the batched
  * launch sequence and their durations accumulate per stage.  Enabling resets the counters. */
-#define NNPGPU_NSTAGES 6 /* 0 neighbours, 1 transpose, 2 descriptors, 3 networks, 4 chain rule, 5 gather+energy */
+#define NNPGPU_NSTAGES 6 /* 0 neighbours, 1 clearing of the force sums, 2 descriptors, 3 networks, 4 chain rule, 5 forces+energy */
 int nnpgpu_profile_enable(nnpgpu_ctx* ctx, int on);
 int nnpgpu_profile_read(const nnpgpu_ctx* ctx, int stage, double* total_ms, long long* count);
 const char* nnpgpu_profile_stage_name(int stage);
