@@ -243,7 +243,9 @@ constexpr int NB_MASK_WORDS = 128;  // structures up to 4096 atoms rank through 
 __host__ __device__ inline size_t nb_warp_smem(int cap) { return (size_t)cap * 24 + 4 * (2 * NB_RANGES + 2 * NB_MASK_WORDS); }
 size_t neighbor_smem_bytes(int cap, int warps) { return (size_t)warps * nb_warp_smem(cap); }
 
-__global__ void __launch_bounds__(128) neighbor_kernel(int a0, int natoms, int cap, double rc, const double* __restrict__ posn,
+// 8 CTAs of 4 warps per SM (64 registers): the candidate loop is latency-bound, and the extra
+// resident warps pay for the few spilled registers
+__global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, int cap, double rc, const double* __restrict__ posn,
                                                        const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
                                                        const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
                                                        const ImgEntry* __restrict__ imgs, const int* __restrict__ atom_cell,
