@@ -14,7 +14,7 @@ namespace nnpgpu {
 // stay in index order.  type_count_kernel counts per block of 256 atoms (warp ballots), the
 // type_offsets_kernel scans the block counts, type_scatter_kernel places each atom
 // at its species offset + its block's offset + its rank within the block.  (The scan runs one
-// warp per species.)
+// warp per species over contiguous runs of block counts per lane.)
 // Layout of tc: [0, NT) counts, [NT_MAX+1, ...) species offsets, [TC_BLK + b*NT_MAX + t) per-block
 // counts (then per-block offsets).
 constexpr int TC_BLK = 3 * NT_MAX + 3;
@@ -41,33 +41,39 @@ __global__ void __launch_bounds__(256) type_count_kernel(int a0, int natoms, int
     tc[TC_BLK + blockIdx.x * NT_MAX + threadIdx.x] = c;
   }
 }
-// one warp per species: warp-wide exclusive scans over the block counts, 32 blocks at a time
+// one warp per species: each lane owns a contiguous run of block counts (its loads independent of
+// one another), the runs' totals are scanned across the warp, and after the species totals are
+// known each lane writes its run's offsets with its species' base folded in
 __global__ void type_offsets_kernel(int ntypes, int nblocks, int* __restrict__ tc) {
   __shared__ int total[NT_MAX];
   const int lane = threadIdx.x & 31, t = threadIdx.x >> 5;
   const int* cnt = tc + TC_BLK;
   int* off = tc + TC_BLK + nblocks * NT_MAX;
-  int run = 0;
+  const int per = (nblocks + 31) / 32, b0 = min(lane * per, nblocks), b1 = min(b0 + per, nblocks);
+  int seg = 0, incl = 0;
   if (t < ntypes) {
-    for (int b0 = 0; b0 < nblocks; b0 += 32) {
-      const int b = b0 + lane;
-      const int v = b < nblocks ? cnt[b * NT_MAX + t] : 0;
-      int incl = v;
+    for (int b = b0; b < b1; ++b) seg += cnt[b * NT_MAX + t];
+    incl = seg;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int x = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += x;
-      }
-      if (b < nblocks) off[b * NT_MAX + t] = run + incl - v;  // offset within the species for now
-      run += __shfl_sync(0xffffffffu, incl, 31);
+    for (int o = 1; o < 32; o <<= 1) {
+      const int x = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += x;
     }
   }
-  if (lane == 0 && t < NT_MAX) total[t] = t < ntypes ? run : 0;
+  if (t < NT_MAX) {
+    const int run = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane == 0) total[t] = t < ntypes ? run : 0;
+  }
   __syncthreads();
-  int base = 0;
-  for (int u = 0; u < t && u < NT_MAX; ++u) base += total[u];
-  if (t < ntypes)
-    for (int b = lane; b < nblocks; b += 32) off[b * NT_MAX + t] += base;
+  if (t < ntypes) {
+    int acc = incl - seg;
+    for (int u = 0; u < t; ++u) acc += total[u];
+    for (int b = b0; b < b1; ++b) {
+      const int v = cnt[b * NT_MAX + t];
+      off[b * NT_MAX + t] = acc;
+      acc += v;
+    }
+  }
   if (threadIdx.x < NT_MAX) {
     int acc = 0;
     for (int u = 0; u < (int)threadIdx.x; ++u) acc += total[u];
@@ -80,6 +86,7 @@ __global__ void type_offsets_kernel(int ntypes, int nblocks, int* __restrict__ t
     tc[NT_MAX + 1 + ntypes] = acc;
   }
 }
+
 __global__ void __launch_bounds__(256) type_scatter_kernel(int a0, int natoms, int ntypes, int nblocks, const int* __restrict__ type,
                                                            const int* __restrict__ tc, int* __restrict__ perm) {
   __shared__ int wcnt[8 * NT_MAX];
