@@ -20,6 +20,10 @@ struct BatchDev {
   const double* posn = nullptr;  // [natoms*3]
   const int* type = nullptr;     // [natoms]
   const int* atom_struc = nullptr;
+  // [natoms] the atom each warp of the neighbour kernel takes: whole structures, those with the
+  // most candidate pairs per centre first, so that no slow structure starts at the end (null:
+  // batch order)
+  const int* nb_order = nullptr;
   const StrucMeta* meta = nullptr;
   const ImgEntry* imgs = nullptr;
   // neighbour lists

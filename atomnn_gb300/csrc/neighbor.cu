@@ -253,10 +253,11 @@ __global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, in
                                                        const float4* __restrict__ sfrac_c, const int4* __restrict__ sfloor_c,
                                                        int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
                                                        unsigned char* __restrict__ nb_t, int* __restrict__ nb_cnt,
-                                                       int* __restrict__ status) {
+                                                       int* __restrict__ status, const int* __restrict__ order) {
   const int lane = threadIdx.x & 31;
   int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
+  if (order) i = order[i];  // whole structures, the slowest first
   const StrucMeta& S = meta[atom_struc[i]];
   // cell-list centres in cell order: the warps of a CTA (and of an SM) then search overlapping
   // stencils and share the candidates' lines in L1
@@ -705,7 +706,7 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   const int blocks = (B.natoms + warps - 1) / warps;
   neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
                                              B.atom_cell, B.cell_start, B.cell_atoms, B.sfrac_c, B.sfloor_c, B.nb_j, B.nb_r, B.nb_code, B.nb_t,
-                                             B.nb_cnt, B.status);
+                                             B.nb_cnt, B.status, B.nb_order);
 }
 
 }  // namespace nnpgpu
