@@ -1269,11 +1269,12 @@ __global__ void __launch_bounds__(128) symm_kernel(const __grid_constant__ PotPa
                                                    const int* __restrict__ type, const int* __restrict__ nb_j,
                                                    const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                                    const int* __restrict__ nb_cnt, float* __restrict__ G, int gstride,
-                                                   float* __restrict__ mom, int mstride) {
+                                                   float* __restrict__ mom, int mstride, const int* __restrict__ order) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
+  int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
+  if (order) i = order[i];  // whole structures, the densest first
   const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, false), cap, NEK, false);
   const int I = clamp_type(type[i], P.ntypes);
   const int n = stage_neighbors(S, i, cap, P.ntypes, type, nb_j, nb_t, nb_r, nb_cnt);
@@ -1361,11 +1362,12 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
                                                     const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                                     const int* __restrict__ nb_cnt, const float* __restrict__ dEdG, int gstride,
                                                     const float* __restrict__ mom, int mstride, const int* __restrict__ nb_code,
-                                                    long long* __restrict__ facc) {
+                                                    long long* __restrict__ facc, const int* __restrict__ order) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
+  int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
   if (i >= a0 + natoms) return;
+  if (order) i = order[i];  // whole structures, the densest first
   const bool kx = GEN && P.kx;  // a compile-time false in the GAUSS-only instances
   const WarpSmem S = carve(smem + warp * warp_smem_floats(cap, NEK, kx, gstride + mstride), cap, NEK, kx);
   float* gm = S.gi + gstride;  // the centre's stored moments

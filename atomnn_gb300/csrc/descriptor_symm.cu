@@ -11,7 +11,7 @@ static void launch_symm_t(const BatchDev& B, const PotParams& P, int warps, cuda
   if (!attr) attr = cudaFuncSetAttribute(symm_kernel<NEK, NZK, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   const size_t sm = symm_smem_bytes(B.cap, NEK, warps);
   symm_kernel<NEK, NZK, GEN><<<(B.natoms + warps - 1) / warps, 32 * warps, sm, st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride);
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.G, B.gstride, B.mom, P.mstride, B.at_order);
 }
 
 // Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).

@@ -24,6 +24,9 @@ struct BatchDev {
   // most candidate pairs per centre first, so that no slow structure starts at the end (null:
   // batch order)
   const int* nb_order = nullptr;
+  // [natoms] the atom each warp of the descriptor and chain-rule kernels takes: whole structures,
+  // the densest (most neighbours per atom) first (null: batch order)
+  const int* at_order = nullptr;
   const StrucMeta* meta = nullptr;
   const ImgEntry* imgs = nullptr;
   // neighbour lists

@@ -330,7 +330,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
        ensure(c, c->eatom, sizeof(float) * N) && ensure(c, c->perm, sizeof(int) * N) &&
        ensure(c, c->type_count, sizeof(int) * type_sort_ints((int)N)) && ensure(c, c->facc, sizeof(long long) * 3 * N) &&
        ensure(c, c->force, sizeof(double) * 3 * N) && ensure(c, c->energy, sizeof(double) * std::max(nstruc, 1)) &&
-       ensure(c, c->status, sizeof(int) * ST_WORDS) && ensure(c, c->nb_order, sizeof(int) * N) && (c->P.mstride == 0 || ensure(c, c->mom, sizeof(float) * N * c->P.mstride));
+       ensure(c, c->status, sizeof(int) * ST_WORDS) && ensure(c, c->nb_order, sizeof(int) * N) && ensure(c, c->at_order, sizeof(int) * N) && (c->P.mstride == 0 || ensure(c, c->mom, sizeof(float) * N * c->P.mstride));
   if (ok && U.ncells > 0) {
     // cell counts must start at zero: fresh memory is cleared, later calls leave them at zero
     const size_t before = c->cell_cnt.bytes;  // a grown buffer is a new allocation
@@ -362,19 +362,33 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
     for (int s : sord)
       for (int a = U.offsets[s]; a < U.offsets[s + 1]; ++a) order.push_back(a);
     order.resize(N, 0);
+    // the descriptor and chain-rule kernels: densest structures first (their cost per atom grows
+    // with the neighbours per atom); isolated structures last
+    for (int s = 0; s < nstruc; ++s) {
+      const StrucMeta& m = U.metas[s];
+      const double* R = m.R;
+      const double vol = std::fabs(R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]));
+      cost[s] = (m.mode != 0 && vol > 0) ? m.natoms / vol : 0.0;
+    }
+    for (int s = 0; s < nstruc; ++s) sord[s] = s;
+    std::stable_sort(sord.begin(), sord.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+    for (int s : sord)
+      for (int a = U.offsets[s]; a < U.offsets[s + 1]; ++a) order.push_back(a);
+    order.resize(2 * N, 0);
   }
   const size_t meta_bytes = sizeof(StrucMeta) * nstruc, img_bytes = sizeof(ImgEntry) * imgs.size(), as_bytes = sizeof(int) * N;
   cudaStreamSynchronize(st);  // the staging buffer may still feed an earlier copy
-  if (!ensure_host(c, c->h_meta, meta_bytes + img_bytes + 2 * as_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
+  if (!ensure_host(c, c->h_meta, meta_bytes + img_bytes + 3 * as_bytes + 64)) return set_error(c, NNPGPU_ERR_OOM, "pinned host allocation failed");
   char* h = (char*)c->h_meta.p;
   std::memcpy(h, U.metas.data(), meta_bytes);
   std::memcpy(h + meta_bytes, imgs.data(), img_bytes);
   std::memcpy(h + meta_bytes + img_bytes, as.data(), as_bytes);
-  std::memcpy(h + meta_bytes + img_bytes + as_bytes, order.data(), as_bytes);
+  std::memcpy(h + meta_bytes + img_bytes + as_bytes, order.data(), 2 * as_bytes);
   cudaMemcpyAsync(c->meta.p, h, meta_bytes, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->imgs.p, h + meta_bytes, img_bytes, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->atom_struc.p, h + meta_bytes + img_bytes, as_bytes, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->nb_order.p, h + meta_bytes + img_bytes + as_bytes, as_bytes, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->at_order.p, h + meta_bytes + img_bytes + 2 * as_bytes, as_bytes, cudaMemcpyHostToDevice, st);
   cudaMemsetAsync(c->status.p, 0, sizeof(int) * ST_WORDS, st);
   MetaCache& m = c->meta_cache;
   m.valid = true;
@@ -432,6 +446,7 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
   B.type_count = (int*)c->type_count.p;
   B.facc = (long long*)c->facc.p;
   B.nb_order = (const int*)c->nb_order.p;
+  B.at_order = (const int*)c->at_order.p;
   B.force = force;
   B.energy = energy;
   B.status = (int*)c->status.p;
@@ -470,7 +485,8 @@ int enqueue(nnpgpu_ctx* c, const Uploaded& U, const BatchDev& Ball, int flags, c
     BatchDev B = Ball;
     B.a0 = U.offsets[s];
     B.natoms = U.offsets[s + 1] - U.offsets[s];
-    B.nb_order = nullptr;  // the order covers the whole batch
+    B.nb_order = nullptr;  // the orders cover the whole batch
+    B.at_order = nullptr;
     B.s0 = s;
     B.nstruc = 1;
     const int rc = run_pipeline(c, B, flags, st);
@@ -620,7 +636,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   c->serving.reset();
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
-                    &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->facc, &c->nb_order, &c->force, &c->energy,
+                    &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->facc, &c->nb_order, &c->at_order, &c->force, &c->energy,
                     &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
                     &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in, &c->tr_fref, &c->tr_t,
                     &c->tr_fatom, &c->tr_fstruc, &c->tr_u, &c->sfrac_c, &c->sfloor_c};
