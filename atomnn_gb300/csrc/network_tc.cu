@@ -17,7 +17,9 @@
 // consecutive along K (leading byte offset 128), 8-row groups SBO = K*16 bytes apart.  The
 // weights of each species are packed once on the host in that layout, one hi/lo block per GEMM;
 // each GEMM's block is brought into shared memory by a 1-D TMA bulk copy (cp.async.bulk) into
-// one of two ping-pong buffers, the next GEMM's block loading while the current one runs.
+// one buffer, requested as soon as the previous GEMM's MMAs have completed, so that it loads while
+// that GEMM's epilogue runs.  One buffer (not two) keeps a CTA at 48 KB of shared memory on
+// 64-wide networks, so that four CTAs share an SM, as many as their TMEM columns allow.
 //
 // Every mbarrier wait is bounded (wait_limit polls, a kernel argument); on timeout the kernel
 // records ERR_TIMEOUT and stops issuing work.  Before it frees its TMEM and leaves, thread 0 waits
@@ -189,7 +191,7 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
                                                             uint32_t tmem_cols, int opk, int pcols, int wait_limit,
                                                             int* __restrict__ status) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
-  __shared__ uint64_t bar_w[2], bar_mma;
+  __shared__ uint64_t bar_w, bar_mma;
   __shared__ uint32_t tmem_slot;
   __shared__ int s_err;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -208,11 +210,10 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
   const int opbytes = TC_M * opk * 2;  // opk: the widest K of any GEMM of the batch's networks
   uint8_t* a_hi = smem_raw;                       // activation operand hi [128 x K]
   uint8_t* a_lo = smem_raw + opbytes;             // activation operand lo
-  uint8_t* wbuf[2] = {smem_raw + 2 * opbytes, smem_raw + 2 * opbytes + ((net.maxblock + 1023) & ~1023)};
+  uint8_t* const wbuf = smem_raw + 2 * opbytes;  // the current GEMM's weight block
 
   if (tid == 0) {
-    mbar_init(&bar_w[0], 1);
-    mbar_init(&bar_w[1], 1);
+    mbar_init(&bar_w, 1);
     mbar_init(&bar_mma, 1);
     s_err = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -231,23 +232,20 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
 
   // thread 0's record of the asynchronous work it issued: a weight copy per buffer and the MMA
   // commit, each with the barrier parity of its completion
-  bool w_pending[2] = {false, false}, mma_pending = false;
-  uint32_t w_par[2] = {0, 0}, mma_par = 0;
-  // weights of GEMM g -> buffer g&1 by one 1-D TMA bulk copy, completion on bar_w[g&1]
+  bool w_pending = false, mma_pending = false;
+  uint32_t w_par = 0, mma_par = 0;
+  // weights of GEMM g -> the weight buffer by one 1-D TMA bulk copy, completion on bar_w
   auto load_w = [&](int g) {
     if (g < ngemm) {
-      w_pending[g & 1] = true;
-      uint64_t* bar = &bar_w[g & 1];
+      w_pending = true;
+      uint64_t* bar = &bar_w;
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(net.bytes[g]) : "memory");
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(wbuf[g & 1])),
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(wbuf)),
                    "l"(net.blob + net.off[g]), "r"(net.bytes[g]), "r"(smem_u32(bar))
                    : "memory");
     }
   };
-  if (tid == 0) {
-    load_w(0);
-    load_w(1);
-  }
+  if (tid == 0) load_w(0);
   // scaled inputs of this thread's atom -> split bf16 operand (zero rows past the tile end)
   {
     const int r = tid;
@@ -274,9 +272,9 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
   // the MMAs completed (or a timeout was recorded); then the next-but-one weights are requested.
   auto gemm = [&](int g, int n, int k) {
     if (s_err == 0 && tid == 0) {
-      if (mbar_wait(&bar_w[g & 1], w_par[g & 1], wait_limit)) {
-        w_pending[g & 1] = false;
-        w_par[g & 1] ^= 1u;
+      if (mbar_wait(&bar_w, w_par, wait_limit)) {
+        w_pending = false;
+        w_par ^= 1u;
       } else {
         s_err = 1;
       }
@@ -284,7 +282,7 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
       if (s_err == 0) {
         const uint32_t idesc = umma_idesc(TC_M, n);
         const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
-        const uint32_t bh = smem_u32(wbuf[g & 1]), bl = bh + (uint32_t)(n * k * 2);
+        const uint32_t bh = smem_u32(wbuf), bl = bh + (uint32_t)(n * k * 2);
         for (int kk = 0; kk < k; kk += 16) {
           // advance by two core matrices (16 k) = 256 bytes along K
           const uint32_t o = (uint32_t)(kk * 16);
@@ -301,7 +299,7 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
           s_err = 1;
         }
       }
-      if (s_err == 0) load_w(g + 2);  // buffer g&1 is free again
+      if (s_err == 0) load_w(g + 1);  // the buffer is free again
     }
     __syncthreads();
     tc_fence_after();
@@ -385,8 +383,7 @@ __global__ void __launch_bounds__(128, 4) network_tc_kernel(const __grid_constan
   // every copy and MMA this CTA issued lands before its shared memory and TMEM are released
   if (tid == 0) {
     bool drained = true;
-    for (int b = 0; b < 2; ++b)
-      if (w_pending[b]) drained = mbar_wait(&bar_w[b], w_par[b], TC_DRAIN_LIMIT) && drained;
+    if (w_pending) drained = mbar_wait(&bar_w, w_par, TC_DRAIN_LIMIT) && drained;
     if (mma_pending) drained = mbar_wait(&bar_mma, mma_par, TC_DRAIN_LIMIT) && drained;
     if (s_err) atomicOr(&status[ST_ERROR], ERR_TIMEOUT);
     if (!drained) atomicOr(&status[ST_ERROR], ERR_DRAIN);
@@ -512,7 +509,7 @@ int launch_network_bf16(const BatchDev& B, const NetsP&, const void* tc, int nty
   }
   const int opk = (kmax + 15) / 16 * 16;
   const int pcols = (kmax + 31) / 32 * 32;
-  int smem = 2 * TC_M * opk * 2 + 2 * wblock;
+  int smem = 2 * TC_M * opk * 2 + wblock;
   // accumulator + one parked derivative block per hidden layer but the last
   const int need = pcols * (1 + (maxl - 2));
   uint32_t cols = 32;
