@@ -148,10 +148,13 @@ struct ImgEntry {
 // Device status words (one int array per context).
 // Forces are summed in 64-bit fixed point with FORCE_FRAC_BITS fractional bits (2^-32 eV/A): each
 // neighbour slot's FP32 contribution is rounded once to that grid, and integer sums are exact and
-// commutative, so a force does not depend on the order in which warps add to it.
+// commutative, so a force does not depend on the order in which warps add to it.  A contribution
+// that is not finite or whose components' magnitudes add up to FORCE_MAX_ABS or more (where the
+// sums could wrap) is reported as ERR_FORCE_RANGE, and the call's results are discarded.
+constexpr float FORCE_MAX_ABS = 1.0e9f;
 constexpr int FORCE_FRAC_BITS = 32;
 enum { ST_MAXCOUNT = 0, ST_ERROR = 2, ST_DEBUG = 8, ST_WORDS = 32 };
-enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_TIMEOUT = 8, ERR_DRAIN = 16 };
+enum { ERR_BAD_POSITION = 1, ERR_BAD_TYPE = 2, ERR_TIMEOUT = 8, ERR_DRAIN = 16, ERR_FORCE_RANGE = 32 };
 
 #ifdef __CUDACC__
 // ---- exact FP64 helpers: fixed evaluation order and no FMA contraction, so that the GPU

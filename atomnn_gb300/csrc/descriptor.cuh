@@ -1362,7 +1362,8 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
                                                     const unsigned char* __restrict__ nb_t, const float4* __restrict__ nb_r,
                                                     const int* __restrict__ nb_cnt, const float* __restrict__ dEdG, int gstride,
                                                     const float* __restrict__ mom, int mstride, const int* __restrict__ nb_code,
-                                                    long long* __restrict__ facc, const int* __restrict__ order) {
+                                                    long long* __restrict__ facc, const int* __restrict__ order,
+                                                    int* __restrict__ status) {
   extern __shared__ float smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int i = a0 + blockIdx.x * (blockDim.x >> 5) + warp;
@@ -1470,8 +1471,12 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
   // minimum-image slot loses it, summed in fixed point (each slot rounded once; the neighbours'
   // adds arrive from other warps in any order, and integer sums do not depend on it)
   long long ox = 0, oy = 0, oz = 0;
+  bool bad = false;
   for (int p = lane; p < n; p += 32) {
-    const long long qx = force_fixed(S.wx[p]), qy = force_fixed(S.wy[p]), qz = force_fixed(S.wz[p]);
+    const float wx = S.wx[p], wy = S.wy[p], wz = S.wz[p];
+    // a NaN or infinity propagates through the sum; the host discards the call's results
+    bad = bad || !(fabsf(wx) + fabsf(wy) + fabsf(wz) < FORCE_MAX_ABS);
+    const long long qx = force_fixed(wx), qy = force_fixed(wy), qz = force_fixed(wz);
     ox += qx;
     oy += qy;
     oz += qz;
@@ -1483,6 +1488,7 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
       red_add(fj + 2, -qz);
     }
   }
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&status[ST_ERROR], ERR_FORCE_RANGE);
   ox = warp_sum_ll(ox);
   oy = warp_sum_ll(oy);
   oz = warp_sum_ll(oz);

@@ -12,7 +12,7 @@ static void launch_force_t(const BatchDev& B, const PotParams& P, int warps, cud
   if (!attr) attr = cudaFuncSetAttribute(force_kernel<NEK, NZK, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   const size_t sm = force_smem_bytes(B.cap, NEK, warps, false, B.gstride + P.mstride);
   force_kernel<NEK, NZK, false><<<(B.natoms + warps - 1) / warps, 32 * warps, sm, st>>>(
-      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.nb_code, B.facc, B.at_order);
+      P, B.a0, B.natoms, B.cap, B.type, B.nb_j, B.nb_t, B.nb_r, B.nb_cnt, B.dEdG, B.gstride, B.mom, P.mstride, B.nb_code, B.facc, B.at_order, B.status);
 }
 
 // Kernel instance covering the potential's largest block grid: (ne, nz) within (2,5), (4,5) or (4,6).

@@ -523,6 +523,8 @@ int check_status(nnpgpu_ctx* c, const int* st_words, int cap) {
   }
   if (st_words[ST_ERROR] & ERR_BAD_POSITION) return set_error(c, NNPGPU_ERR_INVALID, "non-finite atom position");
   if (st_words[ST_ERROR] & ERR_BAD_TYPE) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
+  if (st_words[ST_ERROR] & ERR_FORCE_RANGE)
+    return set_error(c, NNPGPU_ERR_INVALID, "a force contribution is not finite or above 1e9 eV/A (outside the fixed-point force sums)");
   if (st_words[ST_ERROR] & ERR_DRAIN)
     return set_error(c, NNPGPU_ERR_TIMEOUT,
                      "a bounded wait on the device ran out and the kernel's own copies did not finish either (tensor-core network); "

@@ -26,7 +26,8 @@ extern "C" {
 
 /* status codes */
 #define NNPGPU_OK 0
-#define NNPGPU_ERR_INVALID (-1)     /* invalid argument or input (NaN position, bad species, singular cell) */
+#define NNPGPU_ERR_INVALID (-1)     /* invalid argument or input (NaN position, bad species, singular cell, a force
+                                       contribution that is not finite or above 1e9 eV/A) */
 #define NNPGPU_ERR_IO (-2)          /* potential file could not be read (NNP::read throws, src/nnp/nnp.cpp:190) */
 #define NNPGPU_ERR_CUDA (-3)        /* CUDA runtime error, or no usable GPU */
 #define NNPGPU_ERR_OOM (-4)         /* device allocation failed or the HBM budget would be exceeded */

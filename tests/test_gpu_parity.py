@@ -221,6 +221,28 @@ def test_invalid_inputs_rejected(engines):
     assert np.isfinite(e[0])
 
 
+def test_force_range_refused(native_lib, tmp_path):
+    """Forces are summed in 64-bit fixed point (2^-32 eV/A): a slot contribution that is not
+    finite or not below 1e9 eV/A is refused with an error instead of wrapping the integer sums;
+    the next call on the same context is unaffected."""
+    from atomnn_gb300 import engine
+    pot = W.make_potential("small64")
+    pot.nets[0].outw = np.array([1.0e14])  # every force scaled far beyond the range
+    path = str(tmp_path / "huge.nnp")
+    W.write_potential(pot, path)
+    eng = engine.Engine(path)
+    try:
+        s = W.make_structures("small64")[0]
+        for fl in (_flags("ENERGY", "FORCE", "BATCHED"), _flags("ENERGY", "FORCE")):
+            with pytest.raises(engine.NNPGPUError) as ei:
+                eng.compute([s], fl)
+            assert ei.value.code == engine.ERR_INVALID and "fixed-point" in str(ei.value)
+        e, _, _ = eng.compute([s], _flags("ENERGY", "BATCHED"))  # no forces: nothing to refuse
+        assert np.isfinite(e).all() and abs(e[0]) > 1e10
+    finally:
+        eng.close()
+
+
 def test_full_size_properties(engines):
     """At full size (65536-atom cell, 13824-atom supercell) where the oracle is too slow:
     translation invariance, zero net force in wide cells, and extensivity under replication."""
