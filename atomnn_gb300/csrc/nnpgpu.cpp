@@ -197,11 +197,12 @@ void make_meta(const double* cell, int atom0, int natoms, double rc, StrucMeta& 
 static int estimate_cap(const nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell) {
   double best = 16;
   const double rc = c->pot.rc;
+  const double sphere = 4.0 / 3.0 * M_PI * (rc + 0.5) * (rc + 0.5) * (rc + 0.5);
   for (int s = 0; s < nstruc; ++s) {
     const double* R = cell + 9 * s;
     const double vol = std::fabs(R[0] * (R[4] * R[8] - R[7] * R[5]) - R[3] * (R[1] * R[8] - R[7] * R[2]) + R[6] * (R[1] * R[5] - R[4] * R[2]));
     double nb;
-    if (vol > 0) nb = natoms[s] / vol * 4.0 / 3.0 * M_PI * std::pow(rc + 0.5, 3) * 1.1 + 16;
+    if (vol > 0) nb = natoms[s] / vol * sphere * 1.1 + 16;
     else nb = natoms[s];
     best = std::max(best, nb);
   }
@@ -720,9 +721,8 @@ static int compute_impl(nnpgpu_ctx* c, int nstruc, const int* natoms, const doub
   int total = 0;
   for (int s = 0; s < nstruc; ++s) total += natoms ? natoms[s] : 0;
   if (total > 0 && (!posn || !species)) return set_error(c, NNPGPU_ERR_INVALID, "positions or species missing");
-  if (!device_io)
-    for (int a = 0; a < total; ++a)
-      if (species[a] < 0 || species[a] >= c->pot.ntypes) return set_error(c, NNPGPU_ERR_INVALID, "species index out of range");
+  // species outside the potential are flagged on the device (every kernel clamps before it
+  // indexes by species) and fail the call with the same error: no serial pass over the atoms here
   int cap = std::min(256, estimate_cap(c, nstruc, natoms, cell));  // the descriptor kernels take at most 256 slots
   // page-locked caller buffers are read and written by DMA directly; others go through the
   // context's pinned staging buffers
