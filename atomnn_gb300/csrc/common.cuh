@@ -215,6 +215,16 @@ __host__ __device__ inline int pack_code(int t0, int t1, int t2, bool mn) {
 }
 __host__ __device__ inline bool code_min(int c) { return (c >> 30) & 1; }
 __host__ __device__ inline int code_t(int c, int k) { return ((c >> (10 * k)) & 0x3ff) - 512; }
+// The code keeps a slot's lattice translation T modulo 1024 per axis (code_t, in [-512, 512)).  T
+// differs from the difference of the two atoms' integer floors (dfloor = floor_i - floor_j) only by
+// the rounding of Cell::diff and the image shell, far less than 512 cells: the full T is the value
+// congruent to code_t nearest to dfloor.
+__host__ __device__ inline int code_t_full(int c, int k, int dfloor) {
+  const int low = code_t(c, k);
+  const int q = dfloor - low + 512;
+  const int m = q >= 0 ? q / 1024 : -((-q + 1023) / 1024);  // floor(q / 1024)
+  return low + 1024 * m;
+}
 
 #ifdef __CUDACC__
 // Asynchronous 16-byte global -> shared copies (cp.async), committed in groups and waited

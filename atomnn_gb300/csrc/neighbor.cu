@@ -513,12 +513,12 @@ __global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, in
       if (s < ns) {
         const int jl = sj_l[s];
         const int code = sc_l[s];
-        T[0] = code_t(code, 0);
-        T[1] = code_t(code, 1);
-        T[2] = code_t(code, 2);
         j = j0 + jl;
         const float4 sj = sfrac[j];
         const int4 fj = w_floors(sj, sfloor, j);
+        T[0] = code_t_full(code, 0, fi.x - fj.x);
+        T[1] = code_t_full(code, 1, fi.y - fj.y);
+        T[2] = code_t_full(code, 2, fi.z - fj.z);
         // f_i - f_j - T = (s_i - s_j) + (floor_i - floor_j - T): the integer part is exact
         const float d0 = (si.x - sj.x) + (float)(fi.x - fj.x - T[0]);
         const float d1 = (si.y - sj.y) + (float)(fi.y - fj.y - T[1]);

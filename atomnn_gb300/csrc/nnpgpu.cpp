@@ -878,11 +878,13 @@ static int neighbors_impl(nnpgpu_ctx* c, double rc_req, int max_slots, int natom
   launch_neighbors(B, st);
   std::vector<int> hj((size_t)natoms * U.cap), hc((size_t)natoms * U.cap), hn(natoms);
   std::vector<float4> hr((size_t)natoms * U.cap);
+  std::vector<int4> hf(natoms);  // the atoms' integer floors: the codes keep translations modulo 1024
   int hstat[ST_WORDS];
   cudaMemcpyAsync(hj.data(), c->nb_j.p, sizeof(int) * hj.size(), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(hc.data(), c->nb_code.p, sizeof(int) * hc.size(), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(hr.data(), c->nb_r.p, sizeof(float4) * hr.size(), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(hn.data(), c->nb_cnt.p, sizeof(int) * natoms, cudaMemcpyDeviceToHost, st);
+  if (shift) cudaMemcpyAsync(hf.data(), c->sfloor.p, sizeof(int4) * natoms, cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(hstat, c->status.p, sizeof(hstat), cudaMemcpyDeviceToHost, st);
   const cudaError_t e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(c, e, "neighbors");
@@ -897,7 +899,13 @@ static int neighbors_impl(nnpgpu_ctx* c, double rc_req, int max_slots, int natom
       if (index) index[dst] = hj[src];
       if (r) { r[4 * dst] = hr[src].x; r[4 * dst + 1] = hr[src].y; r[4 * dst + 2] = hr[src].z; r[4 * dst + 3] = hr[src].w; }
       if (mn) mn[dst] = code_min(hc[src]) ? 1 : 0;
-      if (shift) for (int x = 0; x < 3; ++x) shift[3 * dst + x] = code_t(hc[src], x);
+      if (shift) {
+        const int j = hj[src];
+        const int4 fi = hf[i], fj = (j >= 0 && j < natoms) ? hf[j] : hf[i];
+        shift[3 * dst] = code_t_full(hc[src], 0, fi.x - fj.x);
+        shift[3 * dst + 1] = code_t_full(hc[src], 1, fi.y - fj.y);
+        shift[3 * dst + 2] = code_t_full(hc[src], 2, fi.z - fj.z);
+      }
     }
   }
   if (status == NNPGPU_OK && hstat[ST_MAXCOUNT] > U.cap)

@@ -176,6 +176,28 @@ def test_cell_list_batch_against_oracle(engines, oracles):
         _assert_ef(e[k], F[k], eo, Fo, s.natoms)
 
 
+def test_far_images_against_oracle(engines, oracles):
+    """Atoms moved by up to 400 lattice vectors (so that their integer floors no longer fit the 9
+    bits packed beside the wrapped coordinates and come from their own array instead), in
+    structures of every neighbour mode (image shells, single image, cell lists) inside one batch:
+    neighbour lists equal the oracle's exactly, energies and forces within the tolerances."""
+    from oracle import pyoracle
+    rng = np.random.default_rng(404)
+    strucs = W.make_structures("mixed512", seed=405, count=6, sizes=[20, 60, 150, 400, 900, 1500])
+    moved = []
+    for k, s in enumerate(strucs):
+        shift = rng.integers(-400, 401, size=(s.natoms, 3)) if k % 2 == 0 else np.zeros((s.natoms, 3), dtype=np.int64)
+        if k == 1:
+            shift[: s.natoms // 2] = 300  # half the atoms far away, half at home
+        moved.append(W.Structure(posn=s.posn + shift @ np.asarray(s.cell).T, species=s.species, cell=s.cell))
+    eng, orc = engines["mixed512"], oracles["mixed512"]
+    e, F, _ = eng.compute(moved, _flags("ENERGY", "FORCE", "BATCHED"))
+    for k, s in enumerate(moved):
+        eo, Fo, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+        _assert_ef(e[k], F[k], eo, Fo, s.natoms)
+        _assert_lists_equal(eng.neighbors(s.posn, s.cell), pyoracle.neighbors(orc.rc, s.posn, s.cell))
+
+
 def test_empty_structures_in_batch(engines, oracles):
     strucs = W.make_structures("mixed512", seed=8, count=3, sizes=[20, 30, 25])
     empty = W.Structure(posn=np.zeros((0, 3)), species=np.zeros(0, np.int32), cell=np.eye(3) * 10)
