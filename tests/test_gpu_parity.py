@@ -111,11 +111,19 @@ def _perfect_lattice():
     return W.Structure(posn=idx * a, species=(np.arange(27) % 3 == 0).astype(np.int32), cell=np.eye(3) * m * a)
 
 
-@pytest.mark.parametrize("case", ["sheared", "perfect", "one_atom", "two_atoms", "isolated", "big_cell"])
+@pytest.mark.parametrize("case", ["sheared", "perfect", "one_atom", "two_atoms", "isolated", "big_cell", "thin_slab", "needle"])
 def test_edge_cases_against_oracle(engines, oracles, case):
     rng = np.random.default_rng(4)
     if case == "sheared":
         s = _sheared_cell(rng)
+    elif case in ("thin_slab", "needle"):
+        # one (slab) or two (needle) short lattice vectors: 6 or 9 image shells along those axes
+        cell = W.lattice(2.2, 16.0, 15.0, 88.0, 93.0, 86.0) if case == "thin_slab" else W.lattice(1.6, 1.9, 60.0, 90.0, 90.0, 75.0)
+        n = 14 if case == "thin_slab" else 8
+        f = rng.uniform(0, 1, size=(n, 3))
+        if case == "needle":  # atoms spread along the long axis, no pair closer than the short vectors
+            f[:, 2] = (np.arange(n) + 0.5) / n + rng.uniform(-0.02, 0.02, size=n)
+        s = W.Structure(posn=f @ cell.T, species=(np.arange(n) % 2).astype(np.int32), cell=cell)
     elif case == "perfect":
         s = _perfect_lattice()
     elif case == "one_atom":
