@@ -97,6 +97,26 @@ def test_resident_md_steps_match_fresh_evaluation(served):
         posn += rng.uniform(-0.02, 0.02, size=posn.shape)  # MD-style step, well inside skin/2
 
 
+def test_resident_md_steps_far_images(served, oracle_lib):
+    """Resident MD-style steps of a structure whose atoms sit up to 400 cells from the home cell:
+    the resident list's lattice translations (kept modulo 1024 in the slot codes) are recovered
+    from the atoms' integer floors, so every step equals a fresh evaluation and the oracle."""
+    from atomnn_gb300 import engine
+    rng = np.random.default_rng(6)
+    base = W.make_structures("mixed512", seed=61, count=1, sizes=[400])[0]
+    posn = base.posn + rng.integers(-400, 401, size=(base.natoms, 3)) @ np.asarray(base.cell).T
+    orc = oracle_lib.OracleNNP(os.path.join(GOLDEN, "mixed512.nnp"))
+    for step in range(3):
+        s = W.Structure(posn=posn.copy(), species=base.species, cell=base.cell)
+        e, F, _ = _wait(served, served.submit(s, key=9), s.natoms)
+        e_ref, F_ref, _ = served.compute([s], engine.ENERGY | engine.FORCE | engine.BATCHED | engine.BF16)
+        assert abs(e - e_ref[0]) / s.natoms <= E_TOL
+        assert np.abs(F - F_ref[0]).max() <= F_TOL
+        posn += rng.uniform(-0.02, 0.02, size=posn.shape)
+    eo, Fo, _ = orc.compute(s.posn, s.species, s.cell, force=True)
+    assert abs(e - eo) / s.natoms <= 1e-3 and np.sqrt(np.mean((F - Fo) ** 2)) <= 1e-3  # BF16 gates
+
+
 def test_oversized_request_refused(native_lib):
     from atomnn_gb300 import engine
     eng = engine.Engine(os.path.join(GOLDEN, "mixed512.nnp"))
