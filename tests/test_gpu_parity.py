@@ -399,6 +399,50 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
         eng.close()
 
 
+@pytest.mark.parametrize("nsp", [3, 4])
+def test_many_species_against_oracle(native_lib, oracle_lib, tmp_path, nsp):
+    """Potentials with three and four species: every radial pair and angular block (moment blocks
+    over more than two neighbour species, which do not share their moments; the first species'
+    own block split at zeta 16), the species carried by the neighbour lists and the species sort
+    of the networks, against the oracle: energies and forces on the FP32 path (batched and one
+    structure at a time), descriptors, and the BF16 path's force RMSE."""
+    from atomnn_gb300 import engine
+    rc = 6.0
+    names = [("A", 24.305, -0.5), ("B", 15.999, -0.25), ("C", 12.011, -0.1), ("D", 1.008, -0.05)][:nsp]
+    pot = W.Potential(rc=W._f6(rc), species=[W.Species(n, m, e) for n, m, e in names])
+    for i in range(nsp):
+        for j in range(nsp):
+            pot.radial[(i, j)] = W.RadialBasis(rc=W._f6(rc), rs=[W._f6(0.0), W._f6(3.0)], eta=[W._f6(0.5), W._f6(0.05)])
+        for j in range(nsp):
+            for k in range(j, nsp):
+                pot.angular[(i, j, k)] = W._angular(rc, [0.005], [1, 2, 4, 16] if j == k == 0 else [1, 2, 4], [1, -1])
+    for i in range(nsp):
+        means = W._estimate_means(pot, i, 0.07, [1.0 / nsp] * nsp)
+        pot.nets[i] = W._make_network(np.random.default_rng(10 + i), pot.ninput(i), [32, 32], means)
+    path = str(tmp_path / ("species%d.nnp" % nsp))
+    W.write_potential(pot, path)
+    eng = engine.Engine(path)
+    orc = oracle_lib.OracleNNP(path)
+    try:
+        rng = np.random.default_rng(100 + nsp)
+        strucs = W.make_structures("mixed512", seed=200 + nsp, count=4, sizes=[30, 150, 700, 1300])
+        strucs = [W.Structure(posn=s.posn, species=rng.integers(0, nsp, size=s.natoms).astype(np.int32), cell=s.cell) for s in strucs]
+        e, F, G = eng.compute(strucs, _flags("ENERGY", "FORCE", "SYMM", "BATCHED"))
+        ep, Fp, _ = eng.compute(strucs, _flags("ENERGY", "FORCE"))
+        eb, Fb, _ = eng.compute(strucs, _flags("ENERGY", "FORCE", "BATCHED", "BF16"))
+        off = 0
+        for k, s in enumerate(strucs):
+            eo, Fo, Go = orc.compute(s.posn, s.species, s.cell, force=True, symm=True)
+            _assert_ef(e[k], F[k], eo, Fo, s.natoms)
+            np.testing.assert_array_equal(F[k], Fp[k])
+            Gs = G[off:off + s.natoms, :Go.shape[1]]
+            off += s.natoms
+            np.testing.assert_allclose(Gs, Go, rtol=0, atol=G_TOL * max(np.abs(Go).max(), 1e-30))
+            assert np.sqrt(np.mean((Fb[k] - Fo) ** 2)) <= 1e-3
+    finally:
+        eng.close()
+
+
 def test_energy_from_stored_descriptors(engines, oracles):
     """nnpgpu_energy_symm: NNP::energy on stored descriptors (nnp.cpp:390-402), as the trainers
     evaluate structures read back from binary files, on the oracle's FP64 descriptors.  With and
