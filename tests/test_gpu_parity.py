@@ -351,7 +351,7 @@ def test_autotune_keeps_results(native_lib):
 
 
 @pytest.mark.parametrize("variant", ["all_moment_blocks", "lambda_above_one", "split_unshared", "split_top8", "split_top32",
-                                     "two_high_levels"])
+                                     "two_high_levels", "mixed_cutoffs"])
 def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant):
     """Blocks with zeta <= 4 and |lambda| <= 1 run through the moment tensors, the others
     through the triplet loop.  all_moment_blocks: every block (the same-species A-A block
@@ -360,7 +360,9 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
     split_unshared: two-width A-A blocks with zeta 1, 2, 4, 16 beside blocks of another width,
     so that no moments are shared; split_top8 and split_top32: top levels zeta 8 and 32 (the
     mixed512 potential itself splits its zeta-16 A-A blocks with shared moments);
-    two_high_levels: zeta 8 and 16 in one block, which keeps the whole block on the triplet loop.
+    two_high_levels: zeta 8 and 16 in one block, which keeps the whole block on the triplet loop;
+    mixed_cutoffs: angular blocks with a TANH cutoff at 5.0 A beside COS radial bases at 6.5 A (no
+    cutoff shared by the centre's bases; neighbours beyond a block's radius add nothing to it).
     All against the oracle on structures with one, few and many neighbours."""
     from atomnn_gb300 import engine
     pot = W.make_potential("mixed512")
@@ -370,6 +372,9 @@ def test_angular_paths_against_oracle(native_lib, oracle_lib, tmp_path, variant)
         elif variant == "lambda_above_one":
             if j != k:
                 pot.angular[(i, j, k)] = W._angular(6.5, [0.005, 0.05], [1, 2, 4], [2, -1])
+        elif variant == "mixed_cutoffs":
+            b = pot.angular[(i, j, k)]
+            b.rc, b.cutname = W._f6(5.0), "TANH"
         elif variant == "split_unshared":
             pot.angular[(i, j, k)] = (W._angular(6.5, [0.005, 0.05], [1, 2, 4, 16], [1, -1]) if j == k == 0 else
                                       W._angular(6.5, [0.02], [1, 2, 4], [1, -1]))
