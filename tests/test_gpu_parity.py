@@ -111,11 +111,22 @@ def _perfect_lattice():
     return W.Structure(posn=idx * a, species=(np.arange(27) % 3 == 0).astype(np.int32), cell=np.eye(3) * m * a)
 
 
-@pytest.mark.parametrize("case", ["sheared", "perfect", "one_atom", "two_atoms", "isolated", "big_cell", "thin_slab", "needle"])
+@pytest.mark.parametrize("case", ["sheared", "perfect", "one_atom", "two_atoms", "isolated", "big_cell", "thin_slab", "needle",
+                                  "left_handed", "one_species"])
 def test_edge_cases_against_oracle(engines, oracles, case):
     rng = np.random.default_rng(4)
     if case == "sheared":
         s = _sheared_cell(rng)
+    elif case == "left_handed":
+        # lattice vectors in left-handed order (negative determinant), 180 atoms: cell lists
+        base = W.make_structures("mixed512", seed=31, count=1, sizes=[180])[0]
+        cell = np.asarray(base.cell)[:, [1, 0, 2]]
+        s = W.Structure(posn=base.posn, species=base.species, cell=cell)
+    elif case == "one_species":
+        # only the second species present: the first one's network tiles, moment sets and
+        # triplet blocks are empty
+        base = W.make_structures("mixed512", seed=32, count=1, sizes=[300])[0]
+        s = W.Structure(posn=base.posn, species=np.ones(base.natoms, np.int32), cell=base.cell)
     elif case in ("thin_slab", "needle"):
         # one (slab) or two (needle) short lattice vectors: 6 or 9 image shells along those axes
         cell = W.lattice(2.2, 16.0, 15.0, 88.0, 93.0, 86.0) if case == "thin_slab" else W.lattice(1.6, 1.9, 60.0, 90.0, 90.0, 75.0)
