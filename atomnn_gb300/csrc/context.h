@@ -81,7 +81,7 @@ struct nnpgpu_ctx {
   int tc_wait_limit = 1 << 22;  // polls of each mbarrier wait of the tensor-core networks (nnpgpu_set_wait_limit)
   // batch buffers
   nnpgpu::DevBuf posn, type, atom_struc, meta, imgs, sfrac, sfloor, nb_j, nb_r, nb_code, nb_cnt, G, dEdG, eatom, perm,
-      type_count, facc, force, energy, status, nb_order, at_order, cell_cnt, cell_start, cell_atoms, atom_cell, mom, nb_t, tr_eref,
+      type_count, facc, force, energy, status, nb_order, at_order, cell_of, cell_cnt, cell_start, cell_atoms, atom_cell, mom, nb_t, tr_eref,
       tr_dcdo, tr_err, tr_part, tr_grad, symm_in, tr_fref, tr_t, tr_fatom, tr_fstruc, tr_u, sfrac_c, sfloor_c;
   nnpgpu::HostBuf h_meta, h_in, h_out;  // pinned staging: geometry, inputs, outputs
   int buf_generation = 0;

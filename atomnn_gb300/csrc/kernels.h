@@ -43,6 +43,7 @@ struct BatchDev {
   int* cell_start = nullptr;  // first slot of each cell in cell_atoms (global atom positions)
   int* cell_atoms = nullptr;  // [natoms] atoms ordered by cell
   int* atom_cell = nullptr;   // [natoms] cell of each atom
+  int* cell_of = nullptr;     // [natoms] cell of each position of cell_atoms
   float4* sfrac_c = nullptr;  // [natoms] sfrac in cell_atoms order
   int4* sfloor_c = nullptr;   // [natoms] sfloor in cell_atoms order
   // descriptors and networks

@@ -130,13 +130,14 @@ __global__ void __launch_bounds__(256) cell_scan_kernel(int s0, const StrucMeta*
 __global__ void cell_fill_kernel(int a0, int natoms, const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
                                  const int* __restrict__ atom_cell, int* __restrict__ cell_cnt, const int* __restrict__ cell_start,
                                  int* __restrict__ cell_atoms, const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
-                                 float4* __restrict__ sfrac_c, int4* __restrict__ sfloor_c) {
+                                 float4* __restrict__ sfrac_c, int4* __restrict__ sfloor_c, int* __restrict__ cell_of) {
   const int i = a0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a0 + natoms) return;
   if (meta[atom_struc[i]].mode != 4) return;
   const int c = atom_cell[i];
   const int pos = cell_start[c] + atomicSub(&cell_cnt[c], 1) - 1;
   cell_atoms[pos] = i;
+  cell_of[pos] = c;
   sfrac_c[pos] = sfrac[i];
   sfloor_c[pos] = sfloor[i];
 }
@@ -253,11 +254,13 @@ __global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, in
                                                        const float4* __restrict__ sfrac_c, const int4* __restrict__ sfloor_c,
                                                        int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
                                                        unsigned char* __restrict__ nb_t, int* __restrict__ nb_cnt,
-                                                       int* __restrict__ status, const int* __restrict__ order) {
+                                                       int* __restrict__ status, const int* __restrict__ order,
+                                                       const int* __restrict__ cell_of) {
   const int lane = threadIdx.x & 31;
   int i = a0 + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= a0 + natoms) return;
   if (order) i = order[i];  // whole structures, the slowest first
+  const int kpos = i;       // for a cell-list structure: the centre's position in cell order
   const StrucMeta& S = meta[atom_struc[i]];
   // cell-list centres in cell order: the warps of a CTA (and of an SM) then search overlapping
   // stencils and share the candidates' lines in L1
@@ -306,7 +309,7 @@ __global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, in
     int* wpre = (int*)(msk + NB_MASK_WORDS);
     const int k = S.reach, nx = S.nc[0], ny = S.nc[1], nz = S.nc[2];
     const int side = 2 * k + 1, nrow = side * side;
-    const int ci = atom_cell[i] - S.cell0;
+    const int ci = cell_of[kpos] - S.cell0;  // read beside cell_atoms[kpos], not after it
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
     // ranges 2q, 2q+1 of row q: start[] is monotone, so a run of cells is one slice of cell_atoms
     int len[4], beg[4];
@@ -397,8 +400,8 @@ __global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, in
       }
       __syncwarp();
     }
-    const float4 si = sfrac[i];
-    const int4 fi = sfloor[i];
+    const float4 si = sfrac_c[kpos];  // the centre's own entries, at its cell-order position
+    const int4 fi = sfloor_c[kpos];
     // candidate qd -> its position in cell_atoms: the last non-empty run starting at or before qd
     auto candidate = [&](int qd) -> int {
       int kr;
@@ -698,7 +701,7 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   if (B.ncells > 0) {
     cell_scan_kernel<<<B.nstruc, 256, 0, st>>>(B.s0, B.meta, B.cell_cnt, B.cell_start);
     cell_fill_kernel<<<(B.natoms + 127) / 128, 128, 0, st>>>(B.a0, B.natoms, B.atom_struc, B.meta, B.atom_cell, B.cell_cnt, B.cell_start,
-                                                             B.cell_atoms, B.sfrac, B.sfloor, B.sfrac_c, B.sfloor_c);
+                                                             B.cell_atoms, B.sfrac, B.sfloor, B.sfrac_c, B.sfloor_c, B.cell_of);
     smem = neighbor_smem_bytes(B.cap, warps);
     static bool attr = false;  // skin lists may ask for up to 1024 slots per atom (106 KB)
     if (!attr) attr = cudaFuncSetAttribute(neighbor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
@@ -706,7 +709,7 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   const int blocks = (B.natoms + warps - 1) / warps;
   neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
                                              B.atom_cell, B.cell_start, B.cell_atoms, B.sfrac_c, B.sfloor_c, B.nb_j, B.nb_r, B.nb_code, B.nb_t,
-                                             B.nb_cnt, B.status, B.nb_order);
+                                             B.nb_cnt, B.status, B.nb_order, B.cell_of);
 }
 
 }  // namespace nnpgpu

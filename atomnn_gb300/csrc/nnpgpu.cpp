@@ -336,7 +336,7 @@ int prepare(nnpgpu_ctx* c, int nstruc, const int* natoms, const double* cell, in
     // cell counts must start at zero: fresh memory is cleared, later calls leave them at zero
     const size_t before = c->cell_cnt.bytes;  // a grown buffer is a new allocation
     ok = ensure(c, c->cell_cnt, sizeof(int) * U.ncells) && ensure(c, c->cell_start, sizeof(int) * U.ncells) &&
-         ensure(c, c->cell_atoms, sizeof(int) * N) && ensure(c, c->atom_cell, sizeof(int) * N) &&
+         ensure(c, c->cell_atoms, sizeof(int) * N) && ensure(c, c->atom_cell, sizeof(int) * N) && ensure(c, c->cell_of, sizeof(int) * N) &&
          ensure(c, c->sfrac_c, sizeof(float4) * N) && ensure(c, c->sfloor_c, sizeof(int4) * N);
     if (ok && c->cell_cnt.bytes != before) cudaMemsetAsync(c->cell_cnt.p, 0, c->cell_cnt.bytes, st);
   }
@@ -435,6 +435,7 @@ BatchDev batch_view(nnpgpu_ctx* c, const Uploaded& U, const double* posn, const 
     B.cell_start = (int*)c->cell_start.p;
     B.cell_atoms = (int*)c->cell_atoms.p;
     B.atom_cell = (int*)c->atom_cell.p;
+    B.cell_of = (int*)c->cell_of.p;
     B.sfrac_c = (float4*)c->sfrac_c.p;
     B.sfloor_c = (int4*)c->sfloor_c.p;
   }
@@ -640,7 +641,7 @@ extern "C" void nnpgpu_destroy(nnpgpu_ctx* c) {
   drop_graphs(c);
   DevBuf* bufs[] = {&c->posn, &c->type, &c->atom_struc, &c->meta, &c->imgs, &c->sfrac, &c->sfloor, &c->nb_j, &c->nb_r, &c->nb_code, &c->nb_cnt,
                     &c->G, &c->dEdG, &c->eatom, &c->perm, &c->type_count, &c->facc, &c->nb_order, &c->at_order, &c->force, &c->energy,
-                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->mom, &c->nb_t,
+                    &c->status, &c->cell_cnt, &c->cell_start, &c->cell_atoms, &c->atom_cell, &c->cell_of, &c->mom, &c->nb_t,
                     &c->tr_eref, &c->tr_dcdo, &c->tr_err, &c->tr_part, &c->tr_grad, &c->symm_in, &c->tr_fref, &c->tr_t,
                     &c->tr_fatom, &c->tr_fstruc, &c->tr_u, &c->sfrac_c, &c->sfloor_c};
   for (DevBuf* b : bufs)
