@@ -249,7 +249,7 @@ size_t neighbor_smem_bytes(int cap, int warps) { return (size_t)warps * nb_warp_
 __global__ void __launch_bounds__(128, 8) neighbor_kernel(int a0, int natoms, int cap, double rc, const double* __restrict__ posn,
                                                        const float4* __restrict__ sfrac, const int4* __restrict__ sfloor,
                                                        const int* __restrict__ atom_struc, const StrucMeta* __restrict__ meta,
-                                                       const ImgEntry* __restrict__ imgs, const int* __restrict__ atom_cell,
+                                                       const ImgEntry* __restrict__ imgs,
                                                        const int* __restrict__ cell_start, const int* __restrict__ cell_atoms,
                                                        const float4* __restrict__ sfrac_c, const int4* __restrict__ sfloor_c,
                                                        int* __restrict__ nb_j, float4* __restrict__ nb_r, int* __restrict__ nb_code,
@@ -708,7 +708,7 @@ void launch_neighbors(const BatchDev& B, cudaStream_t st, int warps) {
   }
   const int blocks = (B.natoms + warps - 1) / warps;
   neighbor_kernel<<<blocks, 32 * warps, smem, st>>>(B.a0, B.natoms, B.cap, B.rc, B.posn, B.sfrac, B.sfloor, B.atom_struc, B.meta, B.imgs,
-                                             B.atom_cell, B.cell_start, B.cell_atoms, B.sfrac_c, B.sfloor_c, B.nb_j, B.nb_r, B.nb_code, B.nb_t,
+                                             B.cell_start, B.cell_atoms, B.sfrac_c, B.sfloor_c, B.nb_j, B.nb_r, B.nb_code, B.nb_t,
                                              B.nb_cnt, B.status, B.nb_order, B.cell_of);
 }
 
