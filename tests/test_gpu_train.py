@@ -108,6 +108,50 @@ def test_train_force_grad_rejects_bad_input(pair):
         eng.train_force_grad(strucs, eref, fref, 1.0, "ASINH", delta=0.0)
 
 
+def _three_species_potential(path):
+    rc = 6.0
+    names = [("A", 24.305, -0.5), ("B", 15.999, -0.25), ("C", 12.011, -0.1)]
+    pot = W.Potential(rc=W._f6(rc), species=[W.Species(n, m, e) for n, m, e in names])
+    for i in range(3):
+        for j in range(3):
+            pot.radial[(i, j)] = W.RadialBasis(rc=W._f6(rc), rs=[W._f6(0.0), W._f6(3.0)], eta=[W._f6(0.5), W._f6(0.05)])
+        for j in range(3):
+            for k in range(j, 3):
+                pot.angular[(i, j, k)] = W._angular(rc, [0.005], [1, 2, 4, 16] if j == k == 0 else [1, 2, 4], [1, -1])
+    for i in range(3):
+        means = W._estimate_means(pot, i, 0.07, [1.0 / 3.0] * 3)
+        pot.nets[i] = W._make_network(np.random.default_rng(20 + i), pot.ninput(i), [16, 16], means)
+    W.write_potential(pot, path)
+    return path
+
+
+def test_three_species_trainers_match_oracle(native_lib, oracle_lib, tmp_path):
+    """Both trainers with a three-species potential (every species' networks and parameter block,
+    moment blocks over three neighbour species): loss and gradient against the oracle."""
+    from atomnn_gb300 import engine
+    path = _three_species_potential(str(tmp_path / "three.nnp"))
+    eng = engine.Engine(path)
+    orc = oracle_lib.OracleNNP(path)
+    try:
+        rng = np.random.default_rng(91)
+        strucs = W.make_structures("mixed512", seed=92, count=4, sizes=[20, 90, 300, 700])
+        strucs = [W.Structure(posn=s.posn, species=rng.integers(0, 3, size=s.natoms).astype(np.int32), cell=s.cell) for s in strucs]
+        ref = [orc.compute(s.posn, s.species, s.cell, force=True) for s in strucs]
+        eref = np.array([r[0] for r in ref]) + rng.normal(0.0, 0.3, size=len(strucs)) * np.array([s.natoms for s in strucs]) ** 0.5
+        fref = [r[1] + rng.normal(0.0, 0.2, r[1].shape) for r in ref]
+        L, r2, g = eng.train_grad(strucs, eref, "MSE")
+        Lo, r2o, go = orc.train_grad(strucs, eref, 0, 1.0)
+        assert g.size == sum(eng.nparams(t) for t in range(3))
+        assert abs(L - Lo) <= 1e-5 * abs(Lo) + 1e-9
+        assert np.abs(g - go).max() <= 1e-4 * np.abs(go).max() + 1e-9
+        L, r2, f2, g = eng.train_force_grad(strucs, eref, fref, 2.0, "MSE")
+        Lo, r2o, f2o, go = orc.train_force_grad(strucs, eref, fref, 2.0, 0, 1.0)
+        assert abs(L - Lo) <= 1e-5 * abs(Lo) + 1e-9 and abs(f2 - f2o) <= 1e-5 * abs(f2o) + 1e-9
+        assert np.abs(g - go).max() <= 2e-4 * np.abs(go).max(), np.abs(g - go).max() / np.abs(go).max()
+    finally:
+        eng.close()
+
+
 def test_set_params_updates_the_device_networks(native_lib, oracle_lib, tmp_path):
     """A trainer's update through nnpgpu_set_params reaches the FP32 and tensor-core networks
     (including launch sequences captured before it): energies and forces equal the oracle's on
