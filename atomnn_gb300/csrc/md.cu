@@ -72,13 +72,23 @@ __global__ void md_sum_kernel(int nb, const double* __restrict__ part, double* _
   out[0] = __dmul_rn(0.5, s);
 }
 
-// largest |x - x0|^2 over the atoms (as float bits: non-negative floats order as ints)
-__global__ void md_disp_kernel(int n, const double* __restrict__ x, const double* __restrict__ x0, unsigned* __restrict__ out) {
+// largest |x' - x0|^2 over the atoms (as float bits: non-negative floats order as ints), where
+// x' are the positions the next md_kick_drift_kernel will write: the same FP64 operations on the
+// same v, F and x, so the skin test of the next step is known when this step's energies are read
+__global__ void md_disp_next_kernel(int n, double hdt, double dt, const double* __restrict__ mass, const double* __restrict__ F,
+                                    const double* __restrict__ v, const double* __restrict__ x, const double* __restrict__ x0,
+                                    unsigned* __restrict__ out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float d2 = 0.f;
   if (i < n) {
-    const double a = x[3 * i] - x0[3 * i], b = x[3 * i + 1] - x0[3 * i + 1], c = x[3 * i + 2] - x0[3 * i + 2];
-    d2 = (float)(a * a + b * b + c * c);
+    const double m = mass[i];
+    double s = 0.0;
+    for (int k = 3 * i; k < 3 * i + 3; ++k) {
+      const double vk = __dadd_rn(v[k], __ddiv_rn(__dmul_rn(hdt, F[k]), m));
+      const double a = __dsub_rn(__dadd_rn(x[k], __dmul_rn(vk, dt)), x0[k]);
+      s = __dadd_rn(s, __dmul_rn(a, a));
+    }
+    d2 = (float)s;
   }
   for (int o = 16; o > 0; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
   if ((threadIdx.x & 31) == 0 && d2 > 0.f) atomicMax(out, __float_as_uint(d2));
@@ -264,23 +274,32 @@ extern "C" int nnpgpu_md_run(nnpgpu_md* s, int nsteps, double* pe, double* ke) {
   const int nb = (n + 255) / 256;
   const double hdt = 0.5 * s->dt;
   const float half_skin2 = (float)(0.25 * s->skin * s->skin * (1.0 - 1e-4));  // FP32 test, conservative
+  // the displacement the first step's drift will give (later steps read theirs with the
+  // previous step's energies)
+  auto enqueue_disp_next = [&]() {
+    cudaMemsetAsync(s->disp, 0, 4, st);
+    md_disp_next_kernel<<<nb, 256, 0, st>>>(n, hdt, s->dt, s->m, s->F, s->v, s->x, s->x0, s->disp);
+    cudaMemcpyAsync(s->h + 2, s->disp, 4, cudaMemcpyDeviceToHost, st);
+  };
+  if (s->use_skin && nsteps > 0) {
+    enqueue_disp_next();
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return md_fail(c, e, "md step");
+  }
   for (int t = 0; t < nsteps; ++t) {
-    // first half-step (Verlet::compute, integrator.cpp:172-177)
-    md_kick_drift_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(n, hdt, s->dt, s->m, s->F, s->v, s->x);
+    bool rebuild = false;
     if (s->use_skin) {
-      cudaMemsetAsync(s->disp, 0, 4, st);
-      md_disp_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, s->x, s->x0, s->disp);
-      cudaMemcpyAsync(s->h + 2, s->disp, 4, cudaMemcpyDeviceToHost, st);
-      const cudaError_t e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) return md_fail(c, e, "md step");
       unsigned bits;
       std::memcpy(&bits, s->h + 2, 4);
       float d2;
       std::memcpy(&d2, &bits, 4);
-      if (d2 > half_skin2) {
-        const int rc = md_build(s);
-        if (rc != NNPGPU_OK) return rc;
-      }
+      rebuild = d2 > half_skin2;
+    }
+    // first half-step (Verlet::compute, integrator.cpp:172-177)
+    md_kick_drift_kernel<<<(3 * n + 255) / 256, 256, 0, st>>>(n, hdt, s->dt, s->m, s->F, s->v, s->x);
+    if (rebuild) {
+      const int rc = md_build(s);
+      if (rc != NNPGPU_OK) return rc;
     }
     // forces (Engine::compute -> PotNNPE::compute)
     const int rc = md_forces(s);
@@ -288,6 +307,7 @@ extern "C" int nnpgpu_md_run(nnpgpu_md* s, int nsteps, double* pe, double* ke) {
     // second half-step and kinetic energy (integrator.cpp:181-189)
     md_kick_kernel<<<nb, 256, 0, st>>>(n, hdt, s->m, s->F, s->v, s->part);
     md_sum_kernel<<<1, 32, 0, st>>>(nb, s->part, s->ke);
+    if (s->use_skin && t + 1 < nsteps) enqueue_disp_next();
     cudaMemcpyAsync(s->h, s->pe, 8, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(s->h + 1, s->ke, 8, cudaMemcpyDeviceToHost, st);
     const cudaError_t e = cudaStreamSynchronize(st);

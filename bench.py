@@ -16,7 +16,9 @@ four steps cover it once; the GPU arm's ``cpu_baseline`` times the same four str
 Besides the headline, the line carries per-configuration figures (``configs``) for the 64-atom
 one-species cell, the 1728-atom two-species cell and the 65,536-atom cell with its 96-128-128-1
 networks: GPU atoms/s of the plain FP32 and the batched BF16 path, the oracle's single-thread
-atoms/s, and the energy and force errors against FP64.
+atoms/s, and the energy and force errors against FP64.  ``md`` gives velocity-Verlet step rates
+on resident device state for the two cells, ``training`` the trainers' batch error and gradient
+over the whole workload, each beside the oracle on one core.
 """
 import argparse
 import json
@@ -311,6 +313,91 @@ def gpu_config_lines(E, device, stream, cpu):
     return out
 
 
+def md_lines(E, device, bf16, cpu):
+    """Velocity-Verlet MD on resident device state (nnpgpu_md_run; the reference's MD job,
+    src/torch/torch.cpp:267-275, with Verlet::compute and PotNNPE::compute) on the 1728-atom and
+    the 65,536-atom cells with their own potentials: host wall clock around nnpgpu_md_run, which
+    returns every step's potential and kinetic energy.  The CPU figure is one force evaluation of
+    the oracle per step on one core (the reference's MD job evaluates one structure in one process),
+    from the per-configuration CPU timings."""
+    out = {}
+    for key, name, nsteps in (("c2_cell1728", "cell1728", 500), ("c4_cell65536", "cell65536", 50)):
+        pot = W.workload_files(name, WORK_DIR)
+        s = W.make_structures(name)[0]
+        n = s.natoms
+        mass = np.where(s.species == 0, 24.305, 15.999) * 1.036427e-4  # amu -> eV ps^2 / A^2
+        vel = np.random.default_rng(5).normal(0.0, 1.0, size=(n, 3)) * np.sqrt(0.025 / mass)[:, None]  # about 300 K
+        eng = E.Engine(pot, device=device)
+        try:
+            md = eng.md(s, mass, 0.0005, skin=1.0, vel=vel, flags=E.BF16 if bf16 else 0)
+            try:
+                md.forces()
+                md.run(20)
+                t0 = time.perf_counter()
+                pe, ke = md.run(nsteps)
+                dt = time.perf_counter() - t0
+                _, _, _, rebuilds = md.state()
+            finally:
+                md.close()
+        finally:
+            eng.close()
+        tot = pe + ke
+        line = {"atoms": n, "steps": nsteps, "ms_per_step": 1000.0 * dt / nsteps, "atom_steps_per_s": n * nsteps / dt,
+                "list_rebuilds": rebuilds, "energy_drift_per_atom": float(np.abs(tot - tot[0]).max() / n),
+                "networks": "BF16 tensor cores" if bf16 else "FP32",
+                "desc": "dt 0.5 fs, 1.0 A skin (the rc+skin list re-decided at rc every step, rebuilt after skin/2), about 300 K"}
+        c = cpu.get(key)
+        if c:
+            per_atom = 1.0 / c["atoms_per_s"]
+            line["cpu_oracle"] = {"atom_steps_per_s": c["atoms_per_s"], "ms_per_step": 1000.0 * per_atom * n, "cores": 1,
+                                  "sample": "one E+F evaluation of the cell per step (" + c["sample"] + ")"}
+        out[key] = line
+    return out
+
+
+def training_lines(E, eng, potpath, strucs):
+    """The trainers' batch error and gradient (nnpgpu_train_grad: NNPTE::error with Cost::grad,
+    src/nnp/nnpte.cpp:870-921; nnpgpu_train_force_grad: NNPTEF::error, src/nnp/nnptef.cpp:1043-1135)
+    over the whole workload through the host-buffer API (host wall clock, mean of 3 calls after one),
+    and the FP64 oracle's same call on one core over every 64th structure by size, with the
+    gradients' agreement on that sample."""
+    from oracle import pyoracle
+    rng = np.random.default_rng(11)
+    e0, F0, _ = eng.compute(strucs, E.ENERGY | E.FORCE)
+    eref = np.array(e0) + rng.normal(0.0, 0.3, size=len(strucs)) * np.array([s.natoms for s in strucs]) ** 0.5
+    fref = [F + rng.normal(0.0, 0.2, F.shape) for F in F0]
+    atoms = sum(s.natoms for s in strucs)
+    one = strata(strucs, 64)[0]
+    pick = [next(k for k, s in enumerate(strucs) if s is x) for x in one]
+    orc = pyoracle.OracleNNP(potpath)
+    out = {}
+    for tag, gpu_call, cpu_call in (
+            ("energy", lambda S, er, fr: eng.train_grad(S, er, "MSE")[-1],
+             lambda S, er, fr: orc.train_grad(S, er, 0, 1.0)[-1]),
+            ("energy_force", lambda S, er, fr: eng.train_force_grad(S, er, fr, 1.0, "MSE")[-1],
+             lambda S, er, fr: orc.train_force_grad(S, er, fr, 1.0, 0, 1.0)[-1])):
+        gpu_call(strucs, eref, fref)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            gpu_call(strucs, eref, fref)
+            ts.append(time.perf_counter() - t0)
+        er1, fr1 = eref[pick], [fref[k] for k in pick]
+        t0 = time.perf_counter()
+        go = cpu_call(one, er1, fr1)
+        tc = time.perf_counter() - t0
+        g = gpu_call(one, er1, fr1)
+        n1 = sum(s.natoms for s in one)
+        out[tag] = {"atoms_per_s": atoms / statistics.mean(ts), "ms_per_call": 1000.0 * statistics.mean(ts),
+                    "structures": len(strucs), "atoms": atoms,
+                    "cpu_oracle": {"atoms_per_s": n1 / tc, "cores": 1,
+                                   "sample": "every 64th structure by size (%d structures, %d atoms), one process" % (len(one), n1)},
+                    "grad_err_vs_oracle": float(np.abs(g - go).max() / np.abs(go).max()),
+                    "desc": "loss MSE%s; batch error and gradient of every network parameter, FP64 reduction" %
+                            (", force weight 1.0" if tag == "energy_force" else "")}
+    return out
+
+
 # ----------------------------------------------------------------------------- native arm
 def main():
     ap = argparse.ArgumentParser()
@@ -328,6 +415,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes (profiling runs)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--serve-seconds", type=float, default=60.0)
+    ap.add_argument("--no-md", action="store_true", help="skip the MD step rates")
+    ap.add_argument("--no-train", action="store_true", help="skip the trainers' timings")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_info()
@@ -624,6 +713,16 @@ def main():
             out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread")}
         if not args.no_configs:
             out["configs"] = gpu_config_lines(E, local, stream, cpu_cfg)
+        if not args.no_md:
+            try:
+                out["md"] = md_lines(E, local, bf16_ok, cpu_cfg)
+            except Exception as ex:  # reported in the line; the headline stands on its own
+                out["md"] = {"error": repr(ex)}
+        if not args.no_train:
+            try:
+                out["training"] = training_lines(E, eng, potpath, strucs)
+            except Exception as ex:
+                out["training"] = {"error": repr(ex)}
         print(json.dumps(out), flush=True)
     eng.close()
     if ws > 1:
