@@ -442,18 +442,23 @@ __global__ void __launch_bounds__(128) train_grad_kernel(const __grid_constant__
       n = r % net.nodes[l];
     }
     const float4* d4 = reinterpret_cast<const float4*>(D[l] + n * TILE);
+    // rows are TILE floats apart, so neighbouring threads (consecutive n, or consecutive m in
+    // the output layer) start at a rotated float4: a quarter-warp then reads 8 distinct bank groups
+    static_assert(((TILE / 4) & (TILE / 4 - 1)) == 0, "the rotation wraps with a mask");
+    const int rot = n + (m > 0 ? m : 0);
     float s = 0.f;
     if (m < 0) {
 #pragma unroll 4
       for (int v = 0; v < TILE / 4; ++v) {
-        const float4 x = d4[v];
+        const float4 x = d4[(v + rot) & (TILE / 4 - 1)];
         s += (x.x + x.y) + (x.z + x.w);
       }
     } else {
       const float4* x4 = reinterpret_cast<const float4*>((l == 0 ? X0 : A[l - 1]) + m * TILE);
 #pragma unroll 4
       for (int v = 0; v < TILE / 4; ++v) {
-        const float4 x = d4[v], y = x4[v];
+        const int u = (v + rot) & (TILE / 4 - 1);
+        const float4 x = d4[u], y = x4[u];
         s = fmaf(x.x, y.x, fmaf(x.y, y.y, fmaf(x.z, y.z, fmaf(x.w, y.w, s))));
       }
     }
@@ -474,10 +479,24 @@ __global__ void train_reduce_kernel(const __grid_constant__ NetsP N, int ntypes,
   const int np = net_params(N.net[t]);
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
+  // 16 rows are loaded before they are added (in tile order): the loads overlap, the sum does not
+  // change
+  constexpr int R = 16;
+  const float* col = partial + (size_t)first * pstride + q;
   double s = 0.0;
-  for (int k = 0; k < ntiles; ++k) s += (double)partial[(size_t)(first + k) * pstride + q];
+  int k = 0;
+  for (; k + R <= ntiles; k += R) {
+    float v[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) v[u] = col[(size_t)(k + u) * pstride];
+#pragma unroll
+    for (int u = 0; u < R; ++u) s += (double)v[u];
+  }
+  for (; k < ntiles; ++k) s += (double)col[(size_t)k * pstride];
   grad[goff + q] = accumulate ? grad[goff + q] + s : s;
 }
+
+constexpr int TRAIN_REDUCE_THREADS = 64;
 
 constexpr int TRAIN_TILE = 64;
 
@@ -503,7 +522,8 @@ int launch_train(const BatchDev& B, const NetsP& N, int ntypes, const double* er
   if (smem > 200 * 1024) return -1;
   train_grad_kernel<TRAIN_TILE><<<train_tiles(B.natoms, ntypes), 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, B.gstride,
                                                                                     B.atom_struc, B.s0, dcdo, partial, pstride);
-  train_reduce_kernel<<<dim3((max_params + 127) / 128, ntypes), 128, 0, st>>>(N, ntypes, TRAIN_TILE, B.type_count, partial, pstride, grad, 0);
+  train_reduce_kernel<<<dim3((max_params + TRAIN_REDUCE_THREADS - 1) / TRAIN_REDUCE_THREADS, ntypes), TRAIN_REDUCE_THREADS, 0, st>>>(
+      N, ntypes, TRAIN_TILE, B.type_count, partial, pstride, grad, 0);
   return 0;
 }
 
@@ -686,13 +706,16 @@ __global__ void __launch_bounds__(128) train_force_kernel(const __grid_constant_
       m = r / net.nodes[l];
       n = r % net.nodes[l];
     }
+    // rotated start per thread: conflict-free reads of rows TILE floats apart (as above)
+    static_assert(((TILE / 4) & (TILE / 4 - 1)) == 0, "the rotation wraps with a mask");
+    const int rot = n + (m > 0 ? m : 0);
     float s = 0.f;
     if (l == L - 1) {
       if (m >= 0) {
         const float4* x4 = reinterpret_cast<const float4*>(TA[H - 1] + m * TILE);
 #pragma unroll 4
         for (int v = 0; v < TILE / 4; ++v) {
-          const float4 x = x4[v];
+          const float4 x = x4[(v + rot) & (TILE / 4 - 1)];
           s += (x.x + x.y) + (x.z + x.w);
         }
         s *= net.outw;
@@ -701,7 +724,7 @@ __global__ void __launch_bounds__(128) train_force_kernel(const __grid_constant_
       const float4* d4 = reinterpret_cast<const float4*>(DP[l] + n * TILE);
 #pragma unroll 4
       for (int v = 0; v < TILE / 4; ++v) {
-        const float4 x = d4[v];
+        const float4 x = d4[(v + rot) & (TILE / 4 - 1)];
         s += (x.x + x.y) + (x.z + x.w);
       }
     } else {
@@ -711,7 +734,8 @@ __global__ void __launch_bounds__(128) train_force_kernel(const __grid_constant_
       const float4* tx4 = reinterpret_cast<const float4*>((l == 0 ? TX0 : TA[l - 1]) + m * TILE);
 #pragma unroll 4
       for (int v = 0; v < TILE / 4; ++v) {
-        const float4 a = dp4[v], b = x4[v], c = dt4[v], d = tx4[v];
+        const int u = (v + rot) & (TILE / 4 - 1);
+        const float4 a = dp4[u], b = x4[u], c = dt4[u], d = tx4[u];
         s = fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, fmaf(a.w, b.w, s))));
         s = fmaf(c.x, d.x, fmaf(c.y, d.y, fmaf(c.z, d.z, fmaf(c.w, d.w, s))));
       }
@@ -746,8 +770,8 @@ int launch_train_force(const BatchDev& B, const NetsP& N, int ntypes, const floa
     attr = cudaFuncSetAttribute(train_force_kernel<TRAIN_FORCE_TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) == cudaSuccess;
   train_force_kernel<TRAIN_FORCE_TILE><<<train_force_tiles(B.natoms, ntypes), 128, smem, st>>>(N, ntypes, B.type_count, B.perm, B.G, U,
                                                                                               B.gstride, partial, pstride);
-  train_reduce_kernel<<<dim3((max_params + 127) / 128, ntypes), 128, 0, st>>>(N, ntypes, TRAIN_FORCE_TILE, B.type_count, partial, pstride,
-                                                                             grad, 1);
+  train_reduce_kernel<<<dim3((max_params + TRAIN_REDUCE_THREADS - 1) / TRAIN_REDUCE_THREADS, ntypes), TRAIN_REDUCE_THREADS, 0, st>>>(
+      N, ntypes, TRAIN_FORCE_TILE, B.type_count, partial, pstride, grad, 1);
   return 0;
 }
 

@@ -363,7 +363,7 @@ def training_lines(E, eng, potpath, strucs):
     gradients' agreement on that sample."""
     from oracle import pyoracle
     rng = np.random.default_rng(11)
-    e0, F0, _ = eng.compute(strucs, E.ENERGY | E.FORCE)
+    e0, F0, _ = eng.compute(strucs, E.ENERGY | E.FORCE | E.BATCHED)
     eref = np.array(e0) + rng.normal(0.0, 0.3, size=len(strucs)) * np.array([s.natoms for s in strucs]) ** 0.5
     fref = [F + rng.normal(0.0, 0.2, F.shape) for F in F0]
     atoms = sum(s.natoms for s in strucs)
@@ -417,11 +417,25 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=60.0)
     ap.add_argument("--no-md", action="store_true", help="skip the MD step rates")
     ap.add_argument("--no-train", action="store_true", help="skip the trainers' timings")
+    ap.add_argument("--training-only", action="store_true", help="print only the trainers' timings (one JSON line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     ws, rank, local = dist_info()
     if args.impl == "reference":
         return run_reference(args, ws, rank)
+    if args.training_only:
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local)
+            from atomnn_gb300 import engine as E
+            potpath = W.workload_files(WORKLOAD, WORK_DIR)
+            eng = E.Engine(potpath, device=local)
+            try:
+                print(json.dumps({"workload": WORKLOAD, "training": training_lines(E, eng, potpath, W.make_structures(WORKLOAD)[:args.count])}),
+                      flush=True)
+            finally:
+                eng.close()
+        return 0
 
     pot = W.make_potential(WORKLOAD)
     potpath = W.workload_files(WORKLOAD, WORK_DIR)
