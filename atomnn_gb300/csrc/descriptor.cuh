@@ -1503,8 +1503,186 @@ __global__ void __launch_bounds__(128, 5) force_kernel(const __grid_constant__ P
 // delta_p = t_i - (min_p ? t_j : 0).  Then for a radial function u_f = -sum_p dG_f/dr (delta_p . u_p)
 // and for an angular one u_f = -sum_triplets (dG_f/dcos dcos + dG_f/dr_a (delta_a . u_a) +
 // dG_f/dr_b (delta_b . u_b)), dcos = delta_a.(u_b - cos u_a)/r_a + delta_b.(u_a - cos u_b)/r_b:
-// minus the tangent of the descriptors along the masked displacement field.  Every angular block
-// takes the triplet loop here (moment blocks included), all families through ang_h.
+// minus the tangent of the descriptors along the masked displacement field.  Blocks that are not
+// GAUSS moment blocks take the triplet loop here, all families through ang_h.
+// Moment blocks of the GAUSS family take the tangent through their moments: G_f = sum_c T[f][c] V[c]
+// with V[e][n] = <M^J_n, M^K_n> (half of it less the j == k terms for J == K), so along the
+// displacements dG_f = sum_c T[f][c] dV[c], dV = <dM^J_n, M^K_n> + <M^J_n, dM^K_n> (halved, less
+// half the diagonal's tangent, for J == K).  Per slot, with dd = u . delta and du = (delta - dd u)/r,
+// the pair weight w = exp(-ie r^alpha) f moves by dw = exp(-ie r^alpha) (f' - ie alpha r^(alpha-1) f) dd
+// and the monomial u^(a,b,c) by a u^(a-1,b,c) du_x + b u^(a,b-1,c) du_y + c u^(a,b,c-1) du_z.
+// Lane groups as in build_moments; M as build_moments writes it, dM likewise, and
+// dDg[(set*ne + e)*(MOM_N+1) + n] the tangent of sum w^2 |u|^2n.
+static __device__ void build_moment_tangents(const WarpSmem& S, const AngP& A, bool cc, int nsets, int lo0, int hi0, int lo1, int hi1,
+                                      float* __restrict__ M, float* __restrict__ dM, float* __restrict__ dDg) {
+  const int lane = threadIdx.x & 31;
+  const int pairs = nsets * A.ne;
+  int L = 32;
+  while (L * pairs > 32) L >>= 1;
+  const int grp = lane / L, sub = lane % L;
+  const bool active = grp < pairs;
+  const int set = active ? grp / A.ne : 0, e = active ? grp % A.ne : 0;
+  const int lo = active ? (set ? lo1 : lo0) : 0, hi = active ? (set ? hi1 : hi0) : 0;
+  float acc[MOM_C], dacc[MOM_C], ddg[MOM_N + 1];
+#pragma unroll
+  for (int r = 0; r < MOM_C; ++r) {
+    acc[r] = 0.f;
+    dacc[r] = 0.f;
+  }
+#pragma unroll
+  for (int n = 0; n <= MOM_N; ++n) ddg[n] = 0.f;
+  const float ie = A.ietap[e];
+  for (int p = lo + sub; p < hi; p += L) {
+    const float d = S.d[p], ux = S.ux[p], uy = S.uy[p], uz = S.uz[p], inv = S.inv[p];
+    const float tx = S.wx[p], ty = S.wy[p], tz = S.wz[p];
+    float f, g;
+    if (cc) {
+      f = S.fc[p];
+      g = S.gc[p];
+    } else {
+      cutoff_fg(A.cut, d, A.rc, A.pirc, A.rci, f, g);
+    }
+    const float h = __expf(-ie * powi(d, A.alpha));
+    const float w = h * f;
+    const float dd = tx * ux + ty * uy + tz * uz;
+    const float dw = h * (g - ie * (float)A.alpha * powi(d, A.alpha - 1) * f) * dd;
+    const float dux = (tx - dd * ux) * inv, duy = (ty - dd * uy) * inv, duz = (tz - dd * uz) * inv;
+    float px[MOM_N + 1], py[MOM_N + 1], pz[MOM_N + 1];
+    px[0] = 1.f;
+    py[0] = 1.f;
+    pz[0] = 1.f;
+#pragma unroll
+    for (int k = 1; k <= MOM_N; ++k) {
+      px[k] = px[k - 1] * ux;
+      py[k] = py[k - 1] * uy;
+      pz[k] = pz[k - 1] * uz;
+    }
+#pragma unroll
+    for (int n = 0; n <= MOM_N; ++n)
+#pragma unroll
+      for (int a = n; a >= 0; --a)
+#pragma unroll
+        for (int b = n - a; b >= 0; --b) {
+          const int c = n - a - b;
+          const float yz = py[b] * pz[c];
+          const float m = px[a] * yz;
+          float dm = 0.f;
+          if (a > 0) dm = fmaf((float)a * px[a - 1] * yz, dux, dm);
+          if (b > 0) dm = fmaf((float)b * px[a] * (py[b - 1] * pz[c]), duy, dm);
+          if (c > 0) dm = fmaf((float)c * px[a] * (py[b] * pz[c - 1]), duz, dm);
+          acc[mom_idx(a, b, c)] = fmaf(w, m, acc[mom_idx(a, b, c)]);
+          dacc[mom_idx(a, b, c)] = fmaf(dw, m, fmaf(w, dm, dacc[mom_idx(a, b, c)]));
+        }
+    // d(w^2 |u|^2n) = 2 w dw |u|^2n + 2 n w^2 |u|^2(n-1) (u . du)
+    const float u2 = ux * ux + uy * uy + uz * uz, udu = ux * dux + uy * duy + uz * duz;
+    float un = 1.f, unm = 0.f;
+#pragma unroll
+    for (int n = 0; n <= MOM_N; ++n) {
+      ddg[n] += 2.0f * w * (dw * un + (float)n * w * unm * udu);
+      unm = un;
+      un *= u2;
+    }
+  }
+  for (int o = L >> 1; o > 0; o >>= 1) {
+#pragma unroll
+    for (int r = 0; r < MOM_C; ++r) {
+      acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+      dacc[r] += __shfl_xor_sync(0xffffffffu, dacc[r], o);
+    }
+#pragma unroll
+    for (int n = 0; n <= MOM_N; ++n) ddg[n] += __shfl_xor_sync(0xffffffffu, ddg[n], o);
+  }
+  if (active && sub == 0) {
+#pragma unroll
+    for (int r = 0; r < MOM_C; ++r) {
+      M[(set * A.ne + e) * MOM_C + r] = acc[r];
+      dM[(set * A.ne + e) * MOM_C + r] = dacc[r];
+    }
+#pragma unroll
+    for (int n = 0; n <= MOM_N; ++n) dDg[(set * A.ne + e) * (MOM_N + 1) + n] = ddg[n];
+  }
+}
+
+// dV of one (J, K) pair of moment sets for width e and degree n
+static __device__ __forceinline__ float mom_tangent_inner(const float* __restrict__ MJ, const float* __restrict__ dMJ, const float* __restrict__ MK,
+                                                   const float* __restrict__ dMK, int n, bool same, float ddiag) {
+  float s = 0.f;
+  for (int r = mom_off(n); r < mom_off(n + 1); ++r) s = fmaf(c_mom_mult[r], fmaf(dMJ[r], MK[r], MJ[r] * dMK[r]), s);
+  return same ? 0.5f * (s - ddiag) : s;
+}
+
+// u_f = -dG_f of one GAUSS moment block (its own moments)
+static __device__ void tangent_mom_block(const WarpSmem& S, const AngP& A, const float* __restrict__ atab, bool cc, bool same, int j0, int nJ,
+                                  int k0, int nK, float* __restrict__ Ui) {
+  const int lane = threadIdx.x & 31;
+  const int ns = same ? 1 : 2, nec = A.ne * MOM_C;
+  float* MS = S.ex;               // [set][e][MOM_C]
+  float* dMS = S.ex + ns * nec;   // [set][e][MOM_C]
+  float* dDg = S.ex + 2 * ns * nec;  // [set][e][MOM_N+1]
+  build_moment_tangents(S, A, cc, ns, j0, j0 + nJ, k0, k0 + nK, MS, dMS, dDg);
+  __syncwarp();
+  float* dV = S.scratch;
+  if (lane < A.ne * (MOM_N + 1)) {
+    const int e = lane / (MOM_N + 1), n = lane % (MOM_N + 1);
+    const int kof = (same ? 0 : nec) + e * MOM_C;
+    dV[lane] = mom_tangent_inner(MS + e * MOM_C, dMS + e * MOM_C, MS + kof, dMS + kof, n, same, dDg[e * (MOM_N + 1) + n]);
+  }
+  __syncwarp();
+  const int w = A.ne * (MOM_N + 1);
+  const float* __restrict__ T = atab + A.tab + A.n;
+  for (int f = lane; f < A.n; f += 32) {
+    float v = 0.f;
+    for (int c = 0; c < w; ++c) v = fmaf(T[f * w + c], dV[c], v);
+    Ui[A.off + f] = -v;
+  }
+  __syncwarp();
+}
+
+// u_f = -dG_f of every moment block of centre type I from the shared moments (all GAUSS)
+static __device__ void tangent_mom_shared(const WarpSmem& S, const PotParams& P, int I, bool cc, float* __restrict__ Ui) {
+  const int lane = threadIdx.x & 31;
+  const AngP& R = P.ang[I][P.mrep[I]];
+  const int ns = P.mns[I], ne = R.ne, nec = ne * MOM_C;
+  const int sp0 = P.msp[I][0], sp1 = ns > 1 ? P.msp[I][1] : sp0;
+  float* MS = S.ex;
+  float* dMS = S.ex + ns * nec;
+  float* dDg = S.ex + 2 * ns * nec;
+  build_moment_tangents(S, R, cc, ns, S.toff[sp0], S.toff[sp0 + 1], S.toff[sp1], S.toff[sp1 + 1], MS, dMS, dDg);
+  __syncwarp();
+  int pk = 0, nk = 0, nb = 0, nf = 0;
+  for (int J = 0; J < P.ntypes; ++J)
+    for (int K = J; K < P.ntypes; ++K) {
+      const AngP& A = P.ang[I][lidx(J, K)];
+      if (A.n == 0 || !A.mom || nb >= 3) continue;
+      pk |= (J | (K << 2)) << (4 * nb);
+      nk |= A.n << (8 * nb);
+      nf += A.n;
+      ++nb;
+    }
+  const int w = ne * (MOM_N + 1);
+  float* dV = S.scratch;
+  for (int t = lane; t < nb * w; t += 32) {
+    const int k = t / w, c = t - k * w, e = c / (MOM_N + 1), n = c - e * (MOM_N + 1);
+    const int J = (pk >> (4 * k)) & 3, K = (pk >> (4 * k + 2)) & 3;
+    const int oJ = mom_set(P, I, J) * nec + e * MOM_C, oK = mom_set(P, I, K) * nec + e * MOM_C;
+    dV[t] = mom_tangent_inner(MS + oJ, dMS + oJ, MS + oK, dMS + oK, n, J == K, dDg[(mom_set(P, I, J) * ne + e) * (MOM_N + 1) + n]);
+  }
+  __syncwarp();
+  for (int t = lane; t < nf; t += 32) {
+    int k = 0, f = t;
+    while (k + 1 < nb && f >= ((nk >> (8 * k)) & 255)) {
+      f -= (nk >> (8 * k)) & 255;
+      ++k;
+    }
+    const AngP& A = P.ang[I][lidx((pk >> (4 * k)) & 3, (pk >> (4 * k + 2)) & 3)];
+    const float* __restrict__ T = P.atab + A.tab + A.n + f * w;
+    float v = 0.f;
+    for (int c = 0; c < w; ++c) v = fmaf(T[c], dV[k * w + c], v);
+    Ui[A.off + f] = -v;
+  }
+  __syncwarp();
+}
+
 template <int NE, int NZ>
 __device__ void tangent_block(const WarpSmem& S, const AngP& A, const Sched& sc, int cap) {
   const int lane = threadIdx.x & 31;
@@ -1638,19 +1816,34 @@ __global__ void __launch_bounds__(128) tangent_kernel(const __grid_constant__ Po
   }
   __syncwarp();
 
-  // angular: every block through the triplet loop
+  // angular: GAUSS moment blocks through their moments (a split block's top level, and every
+  // other block, through the triplet loop)
+  const bool msh = P.msh[I] != 0;
+  bool mgauss = true;  // every moment block of this centre type is GAUSS
+  for (int q = 0; q < P.ntypes * (P.ntypes + 1) / 2; ++q)
+    if (P.ang[I][q].n > 0 && P.ang[I][q].mom && P.ang[I][q].phi != ANG_GAUSS) mgauss = false;
+  if (msh && mgauss) tangent_mom_shared(S, P, I, cc, Ui);
   for (int J = 0; J < P.ntypes; ++J)
     for (int K = J; K < P.ntypes; ++K) {
       const AngP& A = P.ang[I][lidx(J, K)];
       if (A.n == 0) continue;
       const int j0 = S.toff[J], nJ = S.toff[J + 1] - j0;
       const int k0 = S.toff[K], nK = S.toff[K + 1] - k0;
+      const bool by_mom = A.mom && (msh ? mgauss : A.phi == ANG_GAUSS);
+      if (by_mom) {
+        if (!msh) tangent_mom_block(S, A, P.atab, cc, J == K, j0, nJ, k0, nK, Ui);
+        if (!A.top) continue;
+        __syncwarp();
+      }
       block_pair_factors<true>(S, A, j0, j0 + nJ, cap, false);
       if (K != J) block_pair_factors<true>(S, A, k0, k0 + nK, cap, false);
       __syncwarp();
       tangent_block<NEK, NZK>(S, A, make_sched(J, K, j0, nJ, k0, nK), cap);
       __syncwarp();
-      for (int f = lane; f < A.n; f += 32) Ui[A.off + f] = -A.norm * S.scratch[(int)P.atab[A.tab + f]];
+      for (int f = lane; f < A.n; f += 32) {
+        const int cell = (int)P.atab[A.tab + f];
+        if (!by_mom || cell % NZ_MAX == A.nz - 1) Ui[A.off + f] = -A.norm * S.scratch[cell];
+      }
       __syncwarp();
     }
 }
