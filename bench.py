@@ -183,7 +183,7 @@ def run_reference(args, ws, rank):
     if rank != 0:
         return 0
     potpath = W.workload_files(WORKLOAD, WORK_DIR)
-    strucs = W.make_structures(WORKLOAD)
+    strucs = W.make_structures(WORKLOAD)[:args.count]
     procs = os.cpu_count() or 1
     pool = OraclePool(potpath, procs)
     parts = strata(strucs)
@@ -196,13 +196,13 @@ def run_reference(args, ws, rank):
             atoms.append(sum(s.natoms for s in sample))
     pool.close()
     value = sum(atoms) / sum(times)
-    sample_desc = ("each step: one of %d size strata of the 512-structure workload (every %d-th structure by size, %d structures, "
+    sample_desc = ("each step: one of %d size strata of the %d-structure workload (every %d-th structure by size, %d structures, "
                    "about %d atoms), largest first, one process per core; %d consecutive steps cover the workload once"
-                   % (NSTRATA, NSTRATA, len(parts[0]), sum(s.natoms for s in parts[0]), NSTRATA))
+                   % (NSTRATA, len(strucs), NSTRATA, len(parts[0]), sum(s.natoms for s in parts[0]), NSTRATA))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atoms/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000 * statistics.mean(times), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": "%s: %s" % (WORKLOAD, "512 triclinic A/B structures, 16-2048 atoms, 56-64-64-1 networks"),
+            "config": {"workload": "%s: %d triclinic A/B structures, 16-2048 atoms, 56-64-64-1 networks" % (WORKLOAD, len(strucs)),
                        "parallelism": "host cores (process pool)"},
             "cpu_baseline": {"value": value, "unit": "atoms/s", "cores": procs, "kind": "port", "sample": sample_desc},
             "e2e": {"value": value, "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

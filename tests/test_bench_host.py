@@ -72,3 +72,21 @@ def test_clock_samples_parsed(monkeypatch):
     clk = bench.ClockSampler(0).stop()
     assert clk["sm_mhz"] == 2070.0 and clk["sm_max_mhz"] == 2070.0
     assert clk["reasons"] == ["sw_power_cap"] and clk["samples"] == 3
+
+
+def test_reference_arm_line():
+    """bench.py --impl reference on the CPU (the oracle over the host cores) prints one JSON line
+    with the keys of the benchmark contract; a 32-structure workload keeps it short."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "3",
+                          "--count", "32"], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "atoms/s" and d["value"] > 0 and d["higher_is_better"] is True
+    assert d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+    assert d["e2e"] == {"value": d["value"], "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "32 triclinic" in d["config"]["workload"]
