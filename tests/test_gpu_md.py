@@ -100,6 +100,34 @@ def test_md_start_forces_and_energy_conservation(eng, orc):
     assert np.abs(pe - pe[0]).max() / n > 1e-4  # the system does evolve
 
 
+def test_md_bf16_networks_start_and_energy_conservation(native_lib, oracle_lib, tmp_path):
+    """The MD run with tensor-core (BF16 split) networks on the 1728-atom cell and its own
+    potential: the starting energy against the FP64 oracle (1e-5 eV/atom) and the total energy
+    over 300 steps, as for the FP32 networks."""
+    from atomnn_gb300 import engine
+    pot = W.workload_files("cell1728", str(tmp_path))
+    s = W.make_structures("cell1728")[0]
+    n = s.natoms
+    mass = np.where(s.species == 0, 24.305, 15.999) * 1.036427e-4  # amu -> eV ps^2 / A^2
+    rng = np.random.default_rng(5)
+    vel = rng.normal(0.0, 1.0, size=(n, 3)) * np.sqrt(0.025 / mass)[:, None]  # about 300 K
+    e = engine.Engine(pot)
+    try:
+        md = e.md(s, mass, 0.0005, skin=1.0, vel=vel, flags=engine.BF16)
+        try:
+            pe0 = md.forces()
+            pe, ke = md.run(300)
+        finally:
+            md.close()
+    finally:
+        e.close()
+    eo, _, _ = oracle_lib.OracleNNP(pot).compute(s.posn, s.species, s.cell, force=True)
+    assert abs(pe0 - eo) / n <= 1e-5
+    tot = pe + ke
+    assert np.abs(tot - tot[0]).max() / n < 1e-3, (tot.min(), tot.max())
+    assert np.abs(pe - pe[0]).max() / n > 1e-6  # the system does evolve
+
+
 def test_md_invalid_inputs(eng):
     from atomnn_gb300 import engine
     s = W.make_structures("mixed512", seed=9, count=1, sizes=[40])[0]
